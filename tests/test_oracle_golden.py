@@ -1,0 +1,100 @@
+"""Pin the CPU oracle to the reference's own outputs (tests/golden/*.npz).
+
+The fixtures were produced by running the reference engine
+(qmb/_hamiltonian_cpu.cpp through qmb/hamiltonian.py) with
+tests/golden/make_golden.py.  apply_within is compared to 1e-12 of the
+absolute sum of contributions (summation order differs); find_relative with
+the heap rule must reproduce the reference's rows byte for byte.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN_CASES, golden
+
+
+def abs_sum_bound(site, kind, coef, configs_i, psi_i, configs_j, particle_cut):
+    """Per-target sum of |coef*psi| over contributing pairs (the tolerance scale)."""
+    mag_coef = np.zeros_like(coef)
+    mag_coef[:, 0] = np.hypot(coef[:, 0], coef[:, 1])
+    return np.abs(oracle.apply_within(site, kind, mag_coef, configs_i, np.abs(psi_i).astype(np.complex128), configs_j,
+                                      particle_cut))
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_apply_within_matches_reference(case):
+    g = golden(case)
+    pc = int(g["particle_cut"])
+    got = oracle.apply_within(g["site"], g["kind"], g["coef"], g["configs_i"], g["psi_i"], g["configs_j"], pc)
+    ref = g["psi_j"]
+    if case == "edge_duplicates":
+        # duplicate target rows: the reference gives the whole amplitude to one of them
+        rows = [bytes(r) for r in g["configs_j"]]
+        for key in set(rows):
+            where = [k for k, r in enumerate(rows) if r == key]
+            assert np.count_nonzero(ref[where]) <= 1 and np.count_nonzero(got[where]) <= 1
+            np.testing.assert_allclose(got[where].sum(), ref[where].sum(), rtol=0, atol=1e-12 * (1 + abs(ref[where]).sum()))
+        return
+    scale = abs_sum_bound(g["site"], g["kind"], g["coef"], g["configs_i"], g["psi_i"], g["configs_j"], pc)
+    assert np.all(np.abs(got - ref) <= 1e-12 * scale + 1e-300)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_diagonal_matches_reference(case):
+    g = golden(case)
+    pc = int(g["particle_cut"])
+    got = oracle.diagonal_term(g["site"], g["kind"], g["coef"], g["diag_configs"], pc)
+    scale = np.abs(g["coef"]).sum()
+    np.testing.assert_allclose(got, g["diag"], rtol=0, atol=1e-12 * scale)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_find_relative_heap_matches_reference_exactly(case):
+    g = golden(case)
+    pc = int(g["particle_cut"])
+    ex = g.get("configs_exclude")
+    for k in g["counts"]:
+        got = oracle.find_relative(g["site"], g["kind"], g["coef"], g["configs_i"], g["psi_i"], int(k), ex, pc, rule="heap")
+        ref = g[f"relative_{k}"]
+        assert got.shape == ref.shape, (case, k)
+        assert np.array_equal(got, ref), (case, k)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_find_relative_ranked_differs_only_in_boundary_ties(case):
+    """The total-order rule selects the same rows except among records tied at the K-th weight."""
+    g = golden(case)
+    pc = int(g["particle_cut"])
+    ex = g.get("configs_exclude")
+    for k in g["counts"]:
+        ref = g[f"relative_{k}"]
+        got, (wk, above, equal, total) = oracle.find_relative(g["site"], g["kind"], g["coef"], g["configs_i"], g["psi_i"],
+                                                              int(k), ex, pc, rule="ranked")
+        if np.array_equal(got, ref):
+            continue
+        tied = {bytes(r) for r in oracle.rows_with_weight(g["site"], g["kind"], g["coef"], g["configs_i"], g["psi_i"], wk,
+                                                          ex, pc)}
+        a = {bytes(r) for r in got}
+        b = {bytes(r) for r in ref}
+        assert (a ^ b) <= tied, (case, k)
+
+
+def test_apply_term_examples():
+    # a+_3 a_1 on |site1>: parity counts site 0..2 after each operator
+    row = np.array([0b00000010], dtype=np.uint8)
+    ok, parity, out = oracle.apply_term([3, 1, 0, 0], [1, 0, 2, 2], row)
+    assert ok and parity == 0 and out[0] == 0b00001000
+    # a+_3 a_1 on |site0, site1>: a_1 sees site 0 occupied, a+_3 sees site 0 occupied -> parity 0
+    row = np.array([0b00000011], dtype=np.uint8)
+    ok, parity, out = oracle.apply_term([3, 1, 0, 0], [1, 0, 2, 2], row)
+    assert ok and parity == 0 and out[0] == 0b00001001
+    # a+_3 a_1 on |site1, site2>: a+_3 sees site 2 -> parity 1
+    row = np.array([0b00000110], dtype=np.uint8)
+    ok, parity, out = oracle.apply_term([3, 1, 0, 0], [1, 0, 2, 2], row)
+    assert ok and parity == 1 and out[0] == 0b00001100
+    # a+_1 on an occupied site fails
+    ok, _, _ = oracle.apply_term([1, 0, 0, 0], [1, 2, 2, 2], np.array([2], dtype=np.uint8))
+    assert not ok
