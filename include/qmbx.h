@@ -1,0 +1,172 @@
+/*
+ * qmbx — C ABI of the GB300 (sm_103a) second-quantized Hamiltonian engine.
+ *
+ * Drop-in boundary for the four torch operators that the reference declares in
+ * qmb/_hamiltonian.cpp:83-89 and implements in qmb/_hamiltonian_cuda.cu:
+ *
+ *   apply_within(configs_i, psi_i, configs_j, site, kind, coef) -> psi_j
+ *   find_relative(configs_i, psi_i, count_selected, site, kind, coef, configs_exclude) -> configs
+ *   diagonal_term(configs, site, kind, coef) -> psi
+ *   single_relative(configs, site, kind, coef) -> configs
+ *
+ * Conventions (qmb/_hamiltonian_cuda.cu:184-232):
+ *   - configurations are rows of n_qubytes bytes, site s in byte s/8 bit s%8
+ *     (qmb/bitspack.py:8-94); rows need no alignment;
+ *   - amplitudes are complex numbers stored as (real, imaginary) pairs:
+ *     double[n][2] for complex128, float[n][2] for complex64;
+ *   - the term table (site int16[T][4], kind uint8[T][4] with 0 = annihilate,
+ *     1 = create, 2 = empty slot, coef double[T][2]) is compiled once on the
+ *     host by qmbx_table_build into a blob that the caller copies to device
+ *     memory (256-byte aligned) and passes to every device call together with
+ *     its host copy, from which only the header is read;
+ *   - device calls take device pointers, a caller-owned workspace of at least
+ *     the size the matching *_workspace query returns (256-byte aligned), and
+ *     a CUDA stream; they enqueue work on that stream and return without
+ *     synchronising, except where noted;
+ *   - no call allocates device memory;
+ *   - every call returns QMBX_OK or an error status and never traps; the
+ *     message of the last error of the calling thread is qmbx_last_error().
+ *
+ * Limits: 1 <= n_qubytes <= 32 (at most 256 sites); particle_cut 1 (fermions)
+ * or 2 (hard-core bosons); row counts below 2^31.
+ */
+#ifndef QMBX_H
+#define QMBX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* qmbx_stream_t; /* a cudaStream_t; NULL is the legacy default stream */
+
+enum {
+    QMBX_OK = 0,
+    QMBX_ERR_ARGUMENT = 1,  /* invalid argument (sizes, kinds, sites, alignment) */
+    QMBX_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    QMBX_ERR_WORKSPACE = 3, /* workspace smaller than the query asked for */
+    QMBX_ERR_DEVICE = 4,    /* a kernel reported an error status (bounded wait expired, capacity exceeded) */
+};
+
+/* Version of this ABI (major * 10000 + minor * 100 + patch). */
+int qmbx_version(void);
+
+/* Message of the last failed call made by this thread ("" when none). */
+const char* qmbx_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Term table (host only, no GPU needed).
+ * Replaces the term-table handling of qmb/hamiltonian.py:71-102 and the
+ * per-thread term decoding of qmb/_hamiltonian_cuda.cu:54-84.
+ * ------------------------------------------------------------------------- */
+
+/* Bytes of the compiled table for these terms. */
+int qmbx_table_bytes(const int16_t* site, const uint8_t* kind, int64_t n_terms, int32_t n_qubytes,
+                     int32_t particle_cut, uint64_t* bytes);
+
+/* Compile the terms into blob (blob_bytes >= qmbx_table_bytes). */
+int qmbx_table_build(const int16_t* site, const uint8_t* kind, const double* coef, int64_t n_terms, int32_t n_qubytes,
+                     int32_t particle_cut, void* blob, uint64_t blob_bytes);
+
+/* Counts read from a compiled table: [n_terms, live terms, diagonal terms, n_qubytes, particle_cut, n_words]. */
+int qmbx_table_counts(const void* table_host, int64_t counts[6]);
+
+/* ---------------------------------------------------------------------------
+ * apply_within: psi_j[j] = sum over terms t and rows i with t|i> = s|j> of
+ * s * coef_t * psi_i[i].  Replaces apply_within_interface
+ * (qmb/_hamiltonian_cuda.cu:171-274).  Where configs_j repeats a row, the
+ * first occurrence receives the amplitude and the others zero.
+ * same_configs != 0 declares configs_i and configs_j to be the same rows
+ * (configs_j is then ignored), which saves one sort.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, int64_t n_j, uint64_t* bytes);
+
+int qmbx_apply_within(const void* table_host, const void* table_dev, const uint8_t* configs_i, const double* psi_i,
+                      int64_t n_i, const uint8_t* configs_j, int64_t n_j, int32_t same_configs, double* psi_j,
+                      void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
+
+/*
+ * Adjoint of qmbx_apply_within (no counterpart in the reference): with the
+ * same rows, out_i[i] = sum over t and j of conj(s * coef_t) * g_j[j], i.e.
+ * H^dagger applied with the roles of the two row sets swapped.  Every row of
+ * configs_i receives its value; repeated rows of configs_j contribute through
+ * their first occurrence only, matching the forward operator.
+ */
+int qmbx_apply_within_adjoint(const void* table_host, const void* table_dev, const uint8_t* configs_i, int64_t n_i,
+                              const uint8_t* configs_j, const double* g_j, int64_t n_j, int32_t same_configs,
+                              double* out_i, void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
+
+/*
+ * FP32 variants (no counterpart in the reference): complex64 inputs, products
+ * formed with an exact FP32 two-product and accumulated per target with
+ * two-sum compensation.  The result is written as complex128 (the compensated
+ * pair, summed exactly) to out_f64 when it is non-NULL and as complex64 to
+ * out_f32 when that is non-NULL.  include_diagonal = 0 leaves out the terms
+ * that map a row onto itself (their contribution is then added in FP64 by
+ * the caller from qmbx_diagonal_term).
+ */
+int qmbx_apply_within_f32c(const void* table_host, const void* table_dev, const uint8_t* configs_i, const float* psi_i,
+                           int64_t n_i, const uint8_t* configs_j, int64_t n_j, int32_t same_configs,
+                           int32_t include_diagonal, double* out_f64, float* out_f32, void* workspace,
+                           uint64_t workspace_bytes, qmbx_stream_t stream);
+
+int qmbx_apply_within_adjoint_f32c(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                   int64_t n_i, const uint8_t* configs_j, const float* g_j, int64_t n_j,
+                                   int32_t same_configs, int32_t include_diagonal, double* out_f64, float* out_f32,
+                                   void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * diagonal_term: out[c] = sum of s * coef_t over terms with t|c> = s|c>.
+ * Replaces diagonal_term_interface (qmb/_hamiltonian_cuda.cu:710-803).
+ * Needs no workspace.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_diagonal_term(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n, double* out,
+                       qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * find_relative: the count_selected heaviest (term, source) records with
+ * weight |s * coef_t * psi_i|^2 among images not in configs_exclude, records
+ * of weight zero dropped, rows sorted and de-duplicated.  Replaces
+ * find_relative_interface (qmb/_hamiltonian_cuda.cu:551-675).  Records of
+ * equal weight are ranked by the reference's visiting order (term-major),
+ * later first.  out must hold count_selected rows; *n_out receives the row
+ * count.  This call synchronises the stream before it returns (the output
+ * size is data dependent).
+ *
+ * The workspace holds the records near the selection threshold, whose number
+ * is known only after a first pass over the candidates.  When the workspace
+ * is too small the call returns QMBX_ERR_WORKSPACE and stores the bytes it
+ * needs in *workspace_needed (when non-NULL); call again with at least that
+ * much.  qmbx_find_relative_workspace returns a starting size.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_find_relative_workspace(const void* table_host, int64_t n_i, int64_t count_selected, int64_t n_exclude,
+                                 uint64_t* bytes);
+
+int qmbx_find_relative(const void* table_host, const void* table_dev, const uint8_t* configs_i, const double* psi_i,
+                       int64_t n_i, int64_t count_selected, const uint8_t* configs_exclude, int64_t n_exclude,
+                       uint8_t* out, int64_t* n_out, void* workspace, uint64_t workspace_bytes,
+                       uint64_t* workspace_needed, qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * single_relative: for every row, one image outside the row set drawn with
+ * probability proportional to |coef_t| (Efraimidis-Spirakis keys from a
+ * per-term uniform variate derived from seed); all-zero rows where none
+ * exists.  Replaces single_relative_interface
+ * (qmb/_hamiltonian_cuda.cu:907-996).
+ * ------------------------------------------------------------------------- */
+
+int qmbx_single_relative_workspace(const void* table_host, int64_t n, uint64_t* bytes);
+
+int qmbx_single_relative(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n,
+                         uint64_t seed, uint8_t* out, void* workspace, uint64_t workspace_bytes,
+                         qmbx_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMBX_H */

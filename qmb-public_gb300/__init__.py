@@ -1,3 +1,12 @@
-"""GB300-native second-quantized Hamiltonian engine (drop-in for qmb.hamiltonian)."""
+"""GB300-native second-quantized Hamiltonian engine (drop-in for qmb.hamiltonian).
+
+``Hamiltonian`` keeps the reference's constructor and its four operators
+(apply_within, find_relative, diagonal_term, single_relative); the work runs
+in hand-written sm_103a CUDA kernels behind the C ABI of include/qmbx.h.
+"""
 
 from . import bitspack, terms  # noqa: F401
+from .energy import variational_energy  # noqa: F401
+from .hamiltonian import Hamiltonian  # noqa: F401
+
+__all__ = ["Hamiltonian", "variational_energy", "bitspack", "terms"]

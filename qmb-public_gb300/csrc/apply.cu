@@ -1,0 +1,504 @@
+// apply_within (forward and adjoint, FP64 and compensated FP32) and
+// diagonal_term.
+//
+// The reference scatters: one thread per (term, source) pair, a byte-wise
+// binary search of the image among the sorted targets, and FP64 atomics
+// (qmb/_hamiltonian_cuda.cu:86-274).  Here the work is gathered instead: one
+// thread per distinct target row walks the daggered terms, finds the source
+// row among the sorted, de-duplicated sources and accumulates in registers,
+// so no atomics are needed and the summation order is fixed.  The adjoint
+// runs the same walk with the forward terms over the sources.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace qmbx {
+
+int check_table(const void* table_host, const void* table_dev) {
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC || h->version != QMBX_TABLE_VERSION) {
+        return fail(QMBX_ERR_ARGUMENT, "table_host is not a compiled qmbx table");
+    }
+    if (table_dev == nullptr || (reinterpret_cast<uintptr_t>(table_dev) % QMBX_ALIGN) != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "table_dev must be a %d-byte aligned device copy of the table", QMBX_ALIGN);
+    }
+    if (h->n_words < 1 || h->n_words > QMBX_MAX_WORDS) {
+        return fail(QMBX_ERR_ARGUMENT, "table has an unsupported word count %d", h->n_words);
+    }
+    return QMBX_OK;
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// compensated FP32 arithmetic: TwoSum (Knuth) and the FMA two-product
+// (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26(6), 2005).  The _rn intrinsics are never contracted or
+// re-associated by the compiler.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+struct CompSum {
+    float s, c;
+    __device__ __forceinline__ void zero() { s = c = 0.f; }
+    __device__ __forceinline__ void add(float x) {
+        float e;
+        two_sum(s, x, s, e);
+        c = __fadd_rn(c, e);
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// coef (hi/lo split, sign already folded) times psi, added to (re, im) with
+// sign (-1)^parity and optional conjugation of the coefficient.
+template <bool CONJ>
+__device__ __forceinline__ void comp_cmul_add(CompSum& re, CompSum& im, float4 cf, float2 p, int parity) {
+    float chr = cf.x, clr = cf.y, chi = CONJ ? -cf.z : cf.z, cli = CONJ ? -cf.w : cf.w;
+    if (parity) {
+        chr = -chr;
+        clr = -clr;
+        chi = -chi;
+        cli = -cli;
+    }
+    float a, ea, b, eb;
+    // real part: chr*px - chi*py (+ low parts)
+    two_prod(chr, p.x, a, ea);
+    two_prod(chi, p.y, b, eb);
+    re.add(a);
+    re.add(-b);
+    re.c = __fadd_rn(re.c, __fadd_rn(__fsub_rn(ea, eb), __fsub_rn(__fmul_rn(clr, p.x), __fmul_rn(cli, p.y))));
+    // imaginary part: chr*py + chi*px (+ low parts)
+    two_prod(chr, p.y, a, ea);
+    two_prod(chi, p.x, b, eb);
+    im.add(a);
+    im.add(b);
+    im.c = __fadd_rn(im.c, __fadd_rn(__fadd_rn(ea, eb), __fadd_rn(__fmul_rn(clr, p.y), __fmul_rn(cli, p.x))));
+}
+
+// ---------------------------------------------------------------------------
+// visitors
+// ---------------------------------------------------------------------------
+
+// Forward (CONJ = false: targets walk the adjoint part, coef as stored) or
+// adjoint (CONJ = true: sources walk the forward part, coef conjugated).
+// Values of the looked-up rows sit in val[u] for unique key u of lookup.
+template <int W, bool CONJ>
+struct GatherF64 {
+    const uint64_t* lookup;  // sorted unique keys of the looked-up row set
+    const int* n_lookup;
+    const double2* val;      // one amplitude per unique looked-up key
+    const double2* coef;     // coefficients of the walked part
+    const double2* dcoef;    // coefficients of the diagonal part
+    double2* out;
+    const int32_t* out_first;  // forward: row of the first occurrence of each target
+    const int32_t* run_start;  // adjoint: sorted-position runs of each source key
+    const int32_t* run_perm;
+    struct Acc {
+        double re, im, dre, dim;
+        int64_t n;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
+        a.re = a.im = a.dre = a.dim = 0.0;
+        a.n = *n_lookup;
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
+        int64_t pos = find_key<W>(lookup, a.n, img);
+        if (pos < 0) return;
+        double2 cf = __ldg(coef + slot);
+        double2 p = __ldg(val + pos);
+        double ci = CONJ ? -cf.y : cf.y;
+        double re = cf.x * p.x - ci * p.y;
+        double im = cf.x * p.y + ci * p.x;
+        if (parity) {
+            re = -re;
+            im = -im;
+        }
+        a.re += re;
+        a.im += im;
+    }
+    __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
+        double2 cf = __ldg(dcoef + slot);
+        double ci = CONJ ? -cf.y : cf.y;
+        a.dre += parity ? -cf.x : cf.x;
+        a.dim += parity ? -ci : ci;
+    }
+    __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
+        if (a.dre != 0.0 || a.dim != 0.0) {
+            int64_t pos = find_key<W>(lookup, a.n, c);
+            if (pos >= 0) {
+                double2 p = __ldg(val + pos);
+                a.re += a.dre * p.x - a.dim * p.y;
+                a.im += a.dre * p.y + a.dim * p.x;
+            }
+        }
+        double2 r = make_double2(a.re, a.im);
+        if (!CONJ) {
+            out[out_first[u]] = r;
+        } else {
+            for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) out[run_perm[k]] = r;
+        }
+    }
+};
+
+template <int W, bool CONJ>
+struct GatherF32C {
+    const uint64_t* lookup;
+    const int* n_lookup;
+    const float2* val;
+    const float4* coef32;
+    const double2* dcoef;
+    int include_diag;
+    double2* out64;
+    float2* out32;
+    const int32_t* out_first;
+    const int32_t* run_start;
+    const int32_t* run_perm;
+    struct Acc {
+        CompSum re, im;
+        double dre, dim;
+        int64_t n;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
+        a.re.zero();
+        a.im.zero();
+        a.dre = a.dim = 0.0;
+        a.n = *n_lookup;
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
+        int64_t pos = find_key<W>(lookup, a.n, img);
+        if (pos < 0) return;
+        comp_cmul_add<CONJ>(a.re, a.im, __ldg(coef32 + slot), __ldg(val + pos), parity);
+    }
+    __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
+        double2 cf = __ldg(dcoef + slot);
+        double ci = CONJ ? -cf.y : cf.y;
+        a.dre += parity ? -cf.x : cf.x;
+        a.dim += parity ? -ci : ci;
+    }
+    __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
+        double re = a.re.value(), im = a.im.value();
+        if (include_diag && (a.dre != 0.0 || a.dim != 0.0)) {
+            int64_t pos = find_key<W>(lookup, a.n, c);
+            if (pos >= 0) {
+                float2 p = __ldg(val + pos);
+                re += a.dre * (double)p.x - a.dim * (double)p.y;
+                im += a.dre * (double)p.y + a.dim * (double)p.x;
+            }
+        }
+        if (!CONJ) {
+            int32_t r = out_first[u];
+            if (out64) out64[r] = make_double2(re, im);
+            if (out32) out32[r] = make_float2((float)re, (float)im);
+        } else {
+            for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) {
+                int32_t r = run_perm[k];
+                if (out64) out64[r] = make_double2(re, im);
+                if (out32) out32[r] = make_float2((float)re, (float)im);
+            }
+        }
+    }
+};
+
+template <int W>
+struct DiagonalF64 {
+    const double2* dcoef;
+    double2* out;
+    struct Acc {
+        double re, im;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const { a.re = a.im = 0.0; }
+    __device__ __forceinline__ void visit(Acc&, const Key<W>&, const Key<W>&, int, int64_t) const {}
+    __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
+        double2 cf = __ldg(dcoef + slot);
+        a.re += parity ? -cf.x : cf.x;
+        a.im += parity ? -cf.y : cf.y;
+    }
+    __device__ __forceinline__ void finish(Acc& a, int64_t row, const Key<W>&) const {
+        out[row] = make_double2(a.re, a.im);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// per-unique-key amplitudes
+// ---------------------------------------------------------------------------
+
+// Sum of the amplitudes of every row in each unique key's run, in sorted
+// (= original row) order.
+template <class T>
+__global__ void run_sum_kernel(const T* __restrict__ psi, const int32_t* __restrict__ perm,
+                               const int32_t* __restrict__ start, const int* __restrict__ count, T* __restrict__ out) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= *count) return;
+    int32_t a = start[u], b = start[u + 1];
+    double re = 0.0, im = 0.0;
+    for (int32_t k = a; k < b; ++k) {
+        T p = psi[perm[k]];
+        re += (double)p.x;
+        im += (double)p.y;
+    }
+    T r;
+    r.x = re;
+    r.y = im;
+    out[u] = r;
+}
+
+// Amplitude of the first occurrence of each unique key.
+template <class T>
+__global__ void first_value_kernel(const T* __restrict__ psi, const int32_t* __restrict__ first,
+                                   const int* __restrict__ count, T* __restrict__ out) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= *count) return;
+    out[u] = psi[first[u]];
+}
+
+// ---------------------------------------------------------------------------
+// host drivers
+// ---------------------------------------------------------------------------
+
+enum class Prec { F64, F32C };
+
+struct ApplyArgs {
+    const void* table_host;
+    const void* table_dev;
+    const uint8_t* configs_i;
+    int64_t n_i;
+    const uint8_t* configs_j;
+    int64_t n_j;
+    bool same;
+    bool adjoint;
+    Prec prec;
+    const void* in;   // forward: psi_i (n_i); adjoint: g_j (n_j)
+    double2* out64;   // forward: n_j rows; adjoint: n_i rows
+    float2* out32;
+    int include_diag;
+};
+
+template <int W>
+int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
+    const qmbx_table_header* h = header_of(a.table_host);
+    const int nq = h->n_qubytes;
+    RowSet rs_i = take_rowset<W>(ws, a.n_i);
+    RowSet rs_j = a.same ? rs_i : take_rowset<W>(ws, a.n_j);
+    // amplitudes per unique key of the looked-up set
+    const int64_t n_lookup = a.adjoint ? a.n_j : a.n_i;
+    void* uval = a.prec == Prec::F64 ? (void*)ws.take<double2>((uint64_t)(n_lookup > 0 ? n_lookup : 1))
+                                     : (void*)ws.take<float2>((uint64_t)(n_lookup > 0 ? n_lookup : 1));
+    if (ws.base == nullptr) return QMBX_OK;
+    if (!ws.fits()) {
+        return fail(QMBX_ERR_WORKSPACE, "workspace of %llu bytes is smaller than the %llu needed",
+                    (unsigned long long)ws.cap, (unsigned long long)ws.used);
+    }
+    const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
+    if (n_out == 0) return QMBX_OK;
+    if (a.out64) QMBX_CUDA_TRY(cudaMemsetAsync(a.out64, 0, (size_t)n_out * sizeof(double2), s));
+    if (a.out32) QMBX_CUDA_TRY(cudaMemsetAsync(a.out32, 0, (size_t)n_out * sizeof(float2), s));
+    int st;
+    if ((st = build_rowset<W>(a.configs_i, nq, rs_i, s)) != QMBX_OK) return st;
+    if (!a.same && (st = build_rowset<W>(a.configs_j, nq, rs_j, s)) != QMBX_OK) return st;
+    if (n_lookup == 0) return QMBX_OK;
+
+    const RowSet& walk = a.adjoint ? rs_i : rs_j;   // rows whose values are computed
+    const RowSet& look = a.adjoint ? rs_j : rs_i;   // rows whose amplitudes are read
+    const unsigned grid_look = grid_for(n_lookup, kThreads);
+    if (a.prec == Prec::F64) {
+        const double2* in = static_cast<const double2*>(a.in);
+        if (a.adjoint) {
+            first_value_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (double2*)uval);
+        } else {
+            run_sum_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
+                                                                  (double2*)uval);
+        }
+    } else {
+        const float2* in = static_cast<const float2*>(a.in);
+        if (a.adjoint) {
+            first_value_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (float2*)uval);
+        } else {
+            run_sum_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
+                                                                 (float2*)uval);
+        }
+    }
+    QMBX_LAUNCH_CHECK("amplitude gather");
+
+    PartView walk_part = part_view(a.table_host, a.table_dev, a.adjoint ? QMBX_PART_FWD : QMBX_PART_ADJ);
+    PartView diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
+    const int64_t n_walk = walk.n;
+    const unsigned grid = grid_for(n_walk, kThreads);
+    KeyRows<W> src{walk.keys};
+    if (a.prec == Prec::F64) {
+        if (!a.adjoint) {
+            GatherF64<W, false> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
+                                  walk.first, nullptr, nullptr};
+            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+        } else {
+            GatherF64<W, true> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
+                                 nullptr, walk.start, walk.perm};
+            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+        }
+    } else {
+        if (!a.include_diag) diag.n = 0;
+        if (!a.adjoint) {
+            GatherF32C<W, false> v{look.keys,  look.count, (const float2*)uval, walk_part.coef32, diag.coef,
+                                   a.include_diag, a.out64, a.out32, walk.first, nullptr, nullptr};
+            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+        } else {
+            GatherF32C<W, true> v{look.keys, look.count, (const float2*)uval, walk_part.coef32, diag.coef,
+                                  a.include_diag, a.out64, a.out32, nullptr, walk.start, walk.perm};
+            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+        }
+    }
+    QMBX_LAUNCH_CHECK("apply_within enumeration");
+    return QMBX_OK;
+}
+
+int dispatch_apply(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
+    switch (header_of(a.table_host)->n_words) {
+        case 1: return apply_impl<1>(a, ws, s);
+        case 2: return apply_impl<2>(a, ws, s);
+        case 3: return apply_impl<3>(a, ws, s);
+        case 4: return apply_impl<4>(a, ws, s);
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+}
+
+int check_rows(const char* name, const void* p, int64_t n) {
+    if (n < 0 || n >= (int64_t(1) << 31)) return fail(QMBX_ERR_ARGUMENT, "%s: row count %lld out of range", name, (long long)n);
+    if (n > 0 && p == nullptr) return fail(QMBX_ERR_ARGUMENT, "%s must not be NULL", name);
+    return QMBX_OK;
+}
+
+int run_apply(ApplyArgs a, void* workspace, uint64_t workspace_bytes, cudaStream_t s) {
+    clear_error();
+    int st = check_table(a.table_host, a.table_dev);
+    if (st != QMBX_OK) return st;
+    if (a.same) {
+        a.configs_j = a.configs_i;
+        a.n_j = a.n_i;
+    }
+    if ((st = check_rows("configs_i", a.configs_i, a.n_i)) != QMBX_OK) return st;
+    if ((st = check_rows("configs_j", a.configs_j, a.n_j)) != QMBX_OK) return st;
+    const int64_t n_in = a.adjoint ? a.n_j : a.n_i;
+    const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
+    if ((st = check_rows("input amplitudes", a.in, n_in)) != QMBX_OK) return st;
+    if (n_out > 0 && a.out64 == nullptr && a.out32 == nullptr) return fail(QMBX_ERR_ARGUMENT, "no output given");
+    if (workspace == nullptr && workspace_bytes > 0) return fail(QMBX_ERR_ARGUMENT, "workspace is NULL");
+    if (workspace != nullptr && reinterpret_cast<uintptr_t>(workspace) % QMBX_ALIGN != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "workspace must be %d-byte aligned", QMBX_ALIGN);
+    }
+    if (workspace == nullptr) {
+        // a call with no workspace is valid only when nothing needs one
+        Arena probe(nullptr, 0);
+        dispatch_apply(a, probe, s);
+        return fail(QMBX_ERR_WORKSPACE, "workspace of %llu bytes required", (unsigned long long)probe.used);
+    }
+    Arena ws(workspace, workspace_bytes);
+    return dispatch_apply(a, ws, s);
+}
+
+template <int W>
+int diagonal_impl(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n, double2* out,
+                  cudaStream_t s) {
+    const qmbx_table_header* h = header_of(table_host);
+    PartView none = part_view(table_host, table_dev, QMBX_PART_DIAG);
+    none.n = 0;
+    PartView diag = part_view(table_host, table_dev, QMBX_PART_DIAG);
+    DiagonalF64<W> v{diag.coef, out};
+    ByteRows<W> src{configs, h->n_qubytes};
+    enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag);
+    QMBX_LAUNCH_CHECK("diagonal_term enumeration");
+    return QMBX_OK;
+}
+
+}  // namespace
+}  // namespace qmbx
+
+using namespace qmbx;
+
+extern "C" int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, int64_t n_j, uint64_t* bytes) {
+    clear_error();
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    // the largest of the forward / adjoint, FP64 / FP32 layouts (they differ by one value array)
+    ApplyArgs a{};
+    a.table_host = table_host;
+    a.n_i = n_i;
+    a.n_j = n_j;
+    a.same = false;
+    a.prec = Prec::F64;
+    uint64_t most = 0;
+    for (int adj = 0; adj < 2; ++adj) {
+        a.adjoint = adj != 0;
+        Arena probe(nullptr, 0);
+        int st = dispatch_apply(a, probe, nullptr);
+        if (st != QMBX_OK) return st;
+        if (probe.used > most) most = probe.used;
+    }
+    *bytes = most;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_apply_within(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                 const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                                 int32_t same_configs, double* psi_j, void* workspace, uint64_t workspace_bytes,
+                                 qmbx_stream_t stream) {
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F64,
+                psi_i, reinterpret_cast<double2*>(psi_j), nullptr, 1};
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_adjoint(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                         int64_t n_i, const uint8_t* configs_j, const double* g_j, int64_t n_j,
+                                         int32_t same_configs, double* out_i, void* workspace,
+                                         uint64_t workspace_bytes, qmbx_stream_t stream) {
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, true, Prec::F64,
+                g_j, reinterpret_cast<double2*>(out_i), nullptr, 1};
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_f32c(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                      const float* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                                      int32_t same_configs, int32_t include_diagonal, double* out_f64, float* out_f32,
+                                      void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream) {
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F32C,
+                psi_i, reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), include_diagonal};
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_adjoint_f32c(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                              int64_t n_i, const uint8_t* configs_j, const float* g_j, int64_t n_j,
+                                              int32_t same_configs, int32_t include_diagonal, double* out_f64,
+                                              float* out_f32, void* workspace, uint64_t workspace_bytes,
+                                              qmbx_stream_t stream) {
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, true, Prec::F32C,
+                g_j, reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), include_diagonal};
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_diagonal_term(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n,
+                                  double* out, qmbx_stream_t stream) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if ((st = check_rows("configs", configs, n)) != QMBX_OK) return st;
+    if (n > 0 && out == nullptr) return fail(QMBX_ERR_ARGUMENT, "out must not be NULL");
+    if (n == 0) return QMBX_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    double2* o = reinterpret_cast<double2*>(out);
+    switch (header_of(table_host)->n_words) {
+        case 1: return diagonal_impl<1>(table_host, table_dev, configs, n, o, s);
+        case 2: return diagonal_impl<2>(table_host, table_dev, configs, n, o, s);
+        case 3: return diagonal_impl<3>(table_host, table_dev, configs, n, o, s);
+        case 4: return diagonal_impl<4>(table_host, table_dev, configs, n, o, s);
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+}

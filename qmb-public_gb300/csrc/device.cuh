@@ -1,0 +1,331 @@
+// Device-side building blocks shared by the qmbx kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qmbx.h"
+#include "common.h"
+#include "format.h"
+
+#define QMBX_CUDA_TRY(expr)                                                                          \
+    do {                                                                                             \
+        cudaError_t qmbx_err_ = (expr);                                                              \
+        if (qmbx_err_ != cudaSuccess) {                                                              \
+            return ::qmbx::fail(QMBX_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(qmbx_err_)); \
+        }                                                                                            \
+    } while (0)
+
+#define QMBX_LAUNCH_CHECK(what)                                                                          \
+    do {                                                                                                 \
+        cudaError_t qmbx_err_ = cudaGetLastError();                                                      \
+        if (qmbx_err_ != cudaSuccess) {                                                                  \
+            return ::qmbx::fail(QMBX_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(qmbx_err_)); \
+        }                                                                                                \
+    } while (0)
+
+namespace qmbx {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(int64_t n, int per_block) {
+    int64_t g = (n + per_block - 1) / per_block;
+    return (unsigned)(g > 0 ? g : 1);
+}
+
+// ---------------------------------------------------------------------------
+// keys: W big-endian 64-bit words per configuration (see format.h)
+// ---------------------------------------------------------------------------
+
+template <int W>
+struct Key {
+    uint64_t w[W];
+};
+
+template <int W>
+__device__ __forceinline__ Key<W> load_key(const uint64_t* __restrict__ keys, int64_t i) {
+    Key<W> k;
+    if constexpr (W == 2) {
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(keys) + i);
+        k.w[0] = v.x;
+        k.w[1] = v.y;
+    } else if constexpr (W == 4) {
+        ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(keys) + 2 * i);
+        ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(keys) + 2 * i + 1);
+        k.w[0] = a.x;
+        k.w[1] = a.y;
+        k.w[2] = b.x;
+        k.w[3] = b.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < W; ++q) k.w[q] = __ldg(keys + i * W + q);
+    }
+    return k;
+}
+
+template <int W>
+__device__ __forceinline__ void store_key(uint64_t* __restrict__ keys, int64_t i, const Key<W>& k) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) keys[i * W + q] = k.w[q];
+}
+
+// -1, 0, 1 as a is lexicographically below, equal to or above b
+template <int W>
+__device__ __forceinline__ int key_cmp(const Key<W>& a, const Key<W>& b) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        if (a.w[q] != b.w[q]) return a.w[q] < b.w[q] ? -1 : 1;
+    }
+    return 0;
+}
+
+template <int W>
+__device__ __forceinline__ bool key_eq(const Key<W>& a, const Key<W>& b) {
+    bool e = true;
+#pragma unroll
+    for (int q = 0; q < W; ++q) e &= a.w[q] == b.w[q];
+    return e;
+}
+
+// Position of key among n sorted unique keys, or -1.
+template <int W>
+__device__ __forceinline__ int64_t find_key(const uint64_t* __restrict__ keys, int64_t n, const Key<W>& key) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        Key<W> m = load_key<W>(keys, mid);
+        if (key_cmp<W>(m, key) < 0) {
+            lo = mid + 1;
+        } else {
+            hi = mid;
+        }
+    }
+    if (lo < n && key_eq<W>(load_key<W>(keys, lo), key)) return lo;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// term table parts on the device
+// ---------------------------------------------------------------------------
+
+struct PartView {
+    const uint64_t* test;   // [n][2W] mask, val
+    const uint64_t* apply;  // [n][2W] flip, par
+    const double2* coef;
+    const float4* coef32;
+    const int32_t* orig;
+    const float* norm;
+    int64_t n;
+};
+
+inline PartView part_view(const void* table_host, const void* table_dev, int which) {
+    const qmbx_table_header* h = header_of(table_host);
+    const qmbx_table_part& p = h->part[which];
+    const char* base = static_cast<const char*>(table_dev);
+    PartView v;
+    v.test = reinterpret_cast<const uint64_t*>(base + p.off_test);
+    v.apply = reinterpret_cast<const uint64_t*>(base + p.off_apply);
+    v.coef = reinterpret_cast<const double2*>(base + p.off_coef);
+    v.coef32 = reinterpret_cast<const float4*>(base + p.off_coef32);
+    v.orig = reinterpret_cast<const int32_t*>(base + p.off_orig);
+    v.norm = reinterpret_cast<const float*>(base + p.off_norm);
+    v.n = p.n;
+    return v;
+}
+
+int check_table(const void* table_host, const void* table_dev);
+
+// ---------------------------------------------------------------------------
+// the enumeration kernel: every (configuration, term) pair of one or two
+// table parts, terms staged through shared memory tile by tile so that all
+// threads of a block test the same term at the same time (broadcast reads).
+// ---------------------------------------------------------------------------
+
+constexpr int kTermTile = 128;
+
+template <int W>
+struct TermTile {
+    uint64_t m[kTermTile][4 * W];  // mask, val (2W) then flip, par (2W)
+};
+
+template <int W>
+__device__ __forceinline__ void stage_tile(TermTile<W>& tile, const PartView& part, int64_t t0, int count) {
+    // 4W words per term, copied as 16-byte pairs
+    const int pairs_per_term = 2 * W;
+    const int total = count * pairs_per_term;
+    for (int k = threadIdx.x; k < total; k += blockDim.x) {
+        int term = k / pairs_per_term;
+        int pr = k - term * pairs_per_term;
+        const uint64_t* src = pr < W ? part.test + (t0 + term) * 2 * W + 2 * pr
+                                     : part.apply + (t0 + term) * 2 * W + 2 * (pr - W);
+        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(src));
+        tile.m[term][2 * pr] = v.x;
+        tile.m[term][2 * pr + 1] = v.y;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ bool term_applies(const uint64_t* t, const Key<W>& c) {
+    uint64_t bad = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ t[2 * q + 1]) & t[2 * q];
+    return bad == 0;
+}
+
+template <int W>
+__device__ __forceinline__ int term_image(const uint64_t* t, const Key<W>& c, Key<W>& img) {
+    int par = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        img.w[q] = c.w[q] ^ t[2 * W + 2 * q];
+        par += __popcll(c.w[q] & t[2 * W + 2 * q + 1]);
+    }
+    return par & 1;
+}
+
+// Row sources of the enumeration kernel: packed keys, or raw rows packed on the fly.
+template <int W>
+struct KeyRows {
+    const uint64_t* keys;
+    __device__ __forceinline__ Key<W> get(int64_t i) const { return load_key<W>(keys, i); }
+};
+
+template <int W>
+struct ByteRows {
+    const uint8_t* rows;
+    int nq;
+    __device__ __forceinline__ Key<W> get(int64_t i) const {
+        Key<W> k;
+        const uint8_t* r = rows + i * nq;
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            uint64_t w = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                int b = 8 * q + j;
+                uint64_t byte = b < nq ? (uint64_t)r[b] : 0;
+                w |= byte << (8 * (7 - j));
+            }
+            k.w[q] = w;
+        }
+        return k;
+    }
+};
+
+// Visitor protocol:
+//   struct V { struct Acc; init(Acc&, int64_t row, const Key<W>&);
+//              visit(Acc&, const Key<W>& c, const Key<W>& image, int parity, int64_t slot);
+//              visit_diag(Acc&, const Key<W>& c, int parity, int64_t slot);
+//              finish(Acc&, int64_t row, const Key<W>&); }
+// Rows [0, *n_rows) (or [0, n_max) when n_rows is NULL) of src are visited;
+// off holds the terms that change a row, diag the ones that do not.
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const int* __restrict__ n_rows,
+                                                             int64_t n_max, PartView off, PartView diag) {
+    __shared__ TermTile<W> tile;
+    const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
+    if ((int64_t)blockIdx.x * blockDim.x >= n) return;
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = row < n;
+    Key<W> c;
+    if (live) {
+        c = src.get(row);
+    } else {
+#pragma unroll
+        for (int q = 0; q < W; ++q) c.w[q] = 0;
+    }
+    typename V::Acc acc;
+    v.init(acc, row, c);
+    for (int64_t t0 = 0; t0 < off.n; t0 += kTermTile) {
+        int count = (int)(off.n - t0 < kTermTile ? off.n - t0 : kTermTile);
+        __syncthreads();
+        stage_tile<W>(tile, off, t0, count);
+        __syncthreads();
+        if (live) {
+            for (int k = 0; k < count; ++k) {
+                const uint64_t* t = tile.m[k];
+                if (term_applies<W>(t, c)) {
+                    Key<W> img;
+                    int parity = term_image<W>(t, c, img);
+                    v.visit(acc, c, img, parity, t0 + k);
+                }
+            }
+        }
+    }
+    for (int64_t t0 = 0; t0 < diag.n; t0 += kTermTile) {
+        int count = (int)(diag.n - t0 < kTermTile ? diag.n - t0 : kTermTile);
+        __syncthreads();
+        stage_tile<W>(tile, diag, t0, count);
+        __syncthreads();
+        if (live) {
+            for (int k = 0; k < count; ++k) {
+                const uint64_t* t = tile.m[k];
+                if (term_applies<W>(t, c)) {
+                    Key<W> img;
+                    int parity = term_image<W>(t, c, img);
+                    v.visit_diag(acc, c, parity, t0 + k);
+                }
+            }
+        }
+    }
+    if (live) v.finish(acc, row, c);
+}
+
+// ---------------------------------------------------------------------------
+// key utilities implemented in keys.cu (explicitly instantiated for W = 1..4)
+// ---------------------------------------------------------------------------
+
+// rows (n x n_qubytes bytes, any alignment) -> keys (n x W words)
+template <int W>
+int pack_rows(const uint8_t* rows, int64_t n, int n_qubytes, uint64_t* keys, cudaStream_t s);
+
+// keys -> rows; rows beyond *n_rows (when n_rows != NULL) are left untouched
+template <int W>
+int unpack_rows(const uint64_t* keys, const int* n_rows, int64_t n_max, int n_qubytes, uint8_t* rows,
+                cudaStream_t s);
+
+// Scratch of one radix sort of up to n keys.
+struct SortScratch {
+    uint64_t* keys;
+    int32_t* vals;
+    int32_t* counts;
+    int32_t* scan;
+};
+
+template <int W>
+SortScratch take_sort_scratch(Arena& ws, int64_t n);
+
+// Stable LSD radix sort of (key, value) pairs in lexicographic key order over
+// the first n_bytes row bytes (n_bytes passes of 8 bits).  vals_in == NULL
+// sorts the identity permutation.  keys_out/vals_out must not alias the inputs.
+template <int W>
+int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out, int32_t* vals_out, int64_t n,
+               int n_bytes, const SortScratch& sc, cudaStream_t s);
+
+// A sorted, de-duplicated row set (all buffers carved by take_rowset).
+struct RowSet {
+    uint64_t* packed;       // n x W: keys in input row order
+    uint64_t* sorted_keys;  // n x W, sorted (with repeats)
+    int32_t* perm;          // n: original row of each sorted position
+    uint64_t* keys;         // n x W: unique keys (first *count valid)
+    int32_t* first;         // n: original row of the first occurrence of each unique key
+    int32_t* start;         // n + 1: sorted position where each unique key's run starts
+    int* count;             // device int: number of unique keys
+    int32_t* head;
+    int32_t* pos;
+    SortScratch sort;
+    int64_t n;
+};
+
+template <int W>
+RowSet take_rowset(Arena& ws, int64_t n);
+
+template <int W>
+int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s);
+
+// Exclusive prefix sum of n int32 values (in == out allowed); the total goes
+// to *total when non-NULL.  scratch holds scan_scratch(n) int32 values.
+int64_t scan_scratch(int64_t n);
+int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s);
+
+}  // namespace qmbx

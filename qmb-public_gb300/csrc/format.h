@@ -1,0 +1,63 @@
+// Layout of a compiled term table (shared by the host compiler and the kernels).
+//
+// A configuration is held as n_words 64-bit "key words" in big-endian byte
+// order: row byte b sits in word b / 8 at bits (7 - b % 8) * 8 .. +7, so that
+// comparing key words as unsigned integers, word 0 first, is the reference's
+// lexicographic row order (array_less, qmb/_hamiltonian_cuda.cu:13-26) and
+// site s sits at key bit keybit(s) of word s / 64.
+//
+// Every live term t is compiled, for the configuration c it acts on, into
+//   applicable  <=>  ((c ^ val) & mask) == 0           (per word)
+//   image        =   c ^ flip
+//   sign         =   (-1)^(popcount(c & par))          (par == 0 for hard-core bosons)
+// with the constant part of the sign folded into the stored coefficient.
+// This is the closed form of the reference's operator-by-operator walk
+// (qmb/_hamiltonian_cpu.cpp:48-78): the walk's bit tests fix the initial value
+// of every touched site, its writes toggle each touched site once per
+// operator, and its parity is a GF(2)-linear function of the initial
+// configuration.
+//
+// Three parts are stored: the forward part (terms that change the
+// configuration, applied to sources), the adjoint part (the same terms
+// daggered: slots reversed, create <-> annihilate, applied to targets) and
+// the diagonal part (terms whose flip mask is empty).  Terms that can never
+// apply (an operator writing the value a previous operator of the same term
+// left) are dropped.
+#pragma once
+
+#include <stdint.h>
+
+#define QMBX_MAGIC 0x58424D51u  // "QMBX"
+#define QMBX_TABLE_VERSION 2u
+#define QMBX_MAX_WORDS 4
+#define QMBX_ALIGN 256
+
+enum { QMBX_PART_FWD = 0, QMBX_PART_ADJ = 1, QMBX_PART_DIAG = 2, QMBX_PARTS = 3 };
+
+struct qmbx_table_part {
+    int64_t n;            // terms in this part
+    uint64_t off_test;    // uint64[n][2W]  (mask, val) per word
+    uint64_t off_apply;   // uint64[n][2W]  (flip, par) per word
+    uint64_t off_coef;    // double[n][2]   sign-folded coefficient
+    uint64_t off_coef32;  // float[n][4]    (re_hi, re_lo, im_hi, im_lo)
+    uint64_t off_orig;    // int32[n]       index of the term in the input table
+    uint64_t off_norm;    // float[n]       |coef|^2 rounded to FP32
+};
+
+struct qmbx_table_header {
+    uint32_t magic;
+    uint32_t version;
+    int32_t n_qubytes;
+    int32_t particle_cut;
+    int32_t n_words;
+    int32_t n_sites;
+    int64_t n_terms;      // rows of the input table
+    int64_t n_live;       // terms that can apply
+    qmbx_table_part part[QMBX_PARTS];
+    uint64_t total_bytes;
+};
+
+#ifdef __cplusplus
+static inline int qmbx_keyword(int s) { return s >> 6; }
+static inline int qmbx_keybit(int s) { return (7 - ((s >> 3) & 7)) * 8 + (s & 7); }
+#endif

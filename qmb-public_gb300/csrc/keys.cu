@@ -1,0 +1,411 @@
+// Key handling: packing rows into big-endian key words, prefix sums, a stable
+// LSD radix sort, and sorted/de-duplicated row sets.
+//
+// The reference sorts rows with thrust and a byte-wise comparator
+// (qmb/_hamiltonian_cuda.cu:245-251, :624-629, :956-961) and de-duplicates
+// with torch::unique_dim (:666-674); this file does both with its own
+// kernels on 64-bit key words.
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace qmbx {
+
+// ---------------------------------------------------------------------------
+// pack / unpack
+// ---------------------------------------------------------------------------
+
+template <int W>
+__global__ void pack_kernel(const uint8_t* __restrict__ rows, int64_t n, int nq, uint64_t* __restrict__ keys) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t* r = rows + i * nq;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        uint64_t w = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int b = 8 * q + j;
+            uint64_t byte = b < nq ? (uint64_t)r[b] : 0;
+            w |= byte << (8 * (7 - j));
+        }
+        keys[i * W + q] = w;
+    }
+}
+
+template <int W>
+__global__ void unpack_kernel(const uint64_t* __restrict__ keys, const int* __restrict__ n_rows, int64_t n_max, int nq,
+                              uint8_t* __restrict__ rows) {
+    int64_t n = n_rows ? (int64_t)*n_rows : n_max;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint8_t* r = rows + i * nq;
+    for (int b = 0; b < nq; ++b) {
+        uint64_t w = keys[i * W + (b >> 3)];
+        r[b] = (uint8_t)(w >> (8 * (7 - (b & 7))));
+    }
+}
+
+template <int W>
+int pack_rows(const uint8_t* rows, int64_t n, int nq, uint64_t* keys, cudaStream_t s) {
+    if (n == 0) return QMBX_OK;
+    pack_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(rows, n, nq, keys);
+    QMBX_LAUNCH_CHECK("pack_kernel");
+    return QMBX_OK;
+}
+
+template <int W>
+int unpack_rows(const uint64_t* keys, const int* n_rows, int64_t n_max, int nq, uint8_t* rows, cudaStream_t s) {
+    if (n_max == 0) return QMBX_OK;
+    unpack_kernel<W><<<grid_for(n_max, kThreads), kThreads, 0, s>>>(keys, n_rows, n_max, nq, rows);
+    QMBX_LAUNCH_CHECK("unpack_kernel");
+    return QMBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan (reduce, scan of block sums, scan with offsets)
+// ---------------------------------------------------------------------------
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 8;
+constexpr int kScanChunk = kScanThreads * kScanItems;
+
+__global__ void set_zero_kernel(int32_t* p) { *p = 0; }
+
+__global__ void set_int_kernel(int* p, int v) { *p = v; }
+
+__global__ void identity_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in ? in[i] : (int32_t)i;
+}
+
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t v, int32_t* s_warp, int32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < nwarps ? s_warp[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        if (lane < nwarps) s_warp[lane] = w;
+    }
+    __syncthreads();
+    int32_t before = warp > 0 ? s_warp[warp - 1] : 0;
+    if (total) *total = s_warp[nwarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void scan_reduce_kernel(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ sums) {
+    __shared__ int32_t s_warp[32];
+    int64_t base = (int64_t)blockIdx.x * kScanChunk;
+    int32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+        if (i < n) acc += in[i];
+    }
+    int32_t total;
+    block_exclusive_scan(acc, s_warp, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void scan_sums_kernel(int32_t* __restrict__ sums, int64_t nb, int* __restrict__ total_out) {
+    __shared__ int32_t s_warp[32];
+    // each thread scans a contiguous run of per-block sums
+    int64_t per = (nb + blockDim.x - 1) / blockDim.x;
+    int64_t lo = (int64_t)threadIdx.x * per;
+    int64_t hi = lo + per < nb ? lo + per : nb;
+    int32_t local = 0;
+    for (int64_t i = lo; i < hi; ++i) local += sums[i];
+    int32_t total;
+    int32_t before = block_exclusive_scan(local, s_warp, &total);
+    for (int64_t i = lo; i < hi; ++i) {
+        int32_t v = sums[i];
+        sums[i] = before;
+        before += v;
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = total;
+}
+
+__global__ void scan_apply_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                                  const int32_t* __restrict__ sums) {
+    __shared__ int32_t s_warp[32];
+    int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    int32_t v[kScanItems];
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        local += v[k];
+    }
+    int32_t run = block_exclusive_scan(local, s_warp, nullptr) + sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+}
+
+int64_t scan_scratch(int64_t n) {
+    int64_t nb = (n + kScanChunk - 1) / kScanChunk;
+    return nb < 1 ? 1 : nb;
+}
+
+int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s) {
+    int64_t nb = scan_scratch(n);
+    if (n > 0) scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch);
+    else set_zero_kernel<<<1, 1, 0, s>>>(scratch);
+    scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total);
+    if (n > 0) scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, scratch);
+    QMBX_LAUNCH_CHECK("exclusive_scan");
+    return QMBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stable LSD radix sort, 8-bit digits
+// ---------------------------------------------------------------------------
+
+constexpr int kSortWarps = 8;
+constexpr int kSortThreads = kSortWarps * 32;
+constexpr int kSortRounds = 16;  // items per lane
+constexpr int kSortTile = kSortThreads * kSortRounds;
+
+template <int W>
+__device__ __forceinline__ unsigned digit_of(const uint64_t* k, int word, int shift) {
+    return (unsigned)(k[word] >> shift) & 0xffu;
+}
+
+// counts[d * nblocks + b] = items of block b with digit d
+template <int W>
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* __restrict__ keys, int64_t n,
+                                                                 int word, int shift, int32_t* __restrict__ counts,
+                                                                 int nblocks) {
+    __shared__ int32_t hist[256];
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * kSortTile;
+    for (int k = 0; k < kSortRounds; ++k) {
+        int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
+        if (i < n) {
+            unsigned d = (unsigned)(__ldg(keys + i * W + word) >> shift) & 0xffu;
+            atomicAdd(&hist[d], 1);
+        }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) counts[(int64_t)d * nblocks + blockIdx.x] = hist[d];
+}
+
+// Scatter with ranks that keep the input order among equal digits: warp w of
+// a block owns items [w*32*R, (w+1)*32*R) of the block's tile, visited round
+// by round (32 consecutive items per round).
+template <int W>
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint64_t* __restrict__ keys_in,
+                                                                    const int32_t* __restrict__ vals_in,
+                                                                    uint64_t* __restrict__ keys_out,
+                                                                    int32_t* __restrict__ vals_out, int64_t n,
+                                                                    int word, int shift,
+                                                                    const int32_t* __restrict__ offsets, int nblocks) {
+    __shared__ int32_t s_cnt[kSortWarps][256];
+    __shared__ int32_t s_base[256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+        for (int w = 0; w < kSortWarps; ++w) s_cnt[w][d] = 0;
+        s_base[d] = offsets[(int64_t)d * nblocks + blockIdx.x];
+    }
+    __syncthreads();
+    const int64_t wbase = (int64_t)blockIdx.x * kSortTile + (int64_t)warp * 32 * kSortRounds;
+    unsigned dig[kSortRounds];
+    int32_t rank[kSortRounds];
+    const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        int64_t i = wbase + (int64_t)r * 32 + lane;
+        bool valid = i < n;
+        unsigned d = valid ? (unsigned)(__ldg(keys_in + i * W + word) >> shift) & 0xffu : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        int b = 0;
+        if (lane == leader && valid) {
+            b = s_cnt[warp][d];
+            s_cnt[warp][d] = b + __popc(peers);
+        }
+        b = __shfl_sync(0xffffffffu, b, leader);
+        dig[r] = d;
+        rank[r] = b + __popc(peers & lt_mask);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+        int32_t run = 0;
+        for (int w = 0; w < kSortWarps; ++w) {
+            int32_t c = s_cnt[w][d];
+            s_cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortRounds; ++r) {
+        int64_t i = wbase + (int64_t)r * 32 + lane;
+        if (i < n) {
+            unsigned d = dig[r];
+            int64_t dst = (int64_t)s_base[d] + s_cnt[warp][d] + rank[r];
+#pragma unroll
+            for (int q = 0; q < W; ++q) keys_out[dst * W + q] = keys_in[i * W + q];
+            vals_out[dst] = vals_in ? vals_in[i] : (int32_t)i;
+        }
+    }
+}
+
+template <int W>
+static int sort_blocks(int64_t n) {
+    int64_t nb = (n + kSortTile - 1) / kSortTile;
+    return (int)(nb < 1 ? 1 : nb);
+}
+
+template <int W>
+SortScratch take_sort_scratch(Arena& ws, int64_t n) {
+    SortScratch sc;
+    int nblocks = sort_blocks<W>(n);
+    uint64_t cap = (uint64_t)(n > 0 ? n : 1);
+    sc.keys = ws.take<uint64_t>(cap * W);
+    sc.vals = ws.take<int32_t>(cap);
+    sc.counts = ws.take<int32_t>((uint64_t)256 * nblocks);
+    sc.scan = ws.take<int32_t>((uint64_t)scan_scratch((int64_t)256 * nblocks));
+    return sc;
+}
+
+template <int W>
+int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_out, int32_t* vals_out, int64_t n,
+               int n_bytes, const SortScratch& sc, cudaStream_t s) {
+    if (n == 0) return QMBX_OK;
+    const int nblocks = sort_blocks<W>(n);
+    if (n_bytes == 0) {
+        QMBX_CUDA_TRY(cudaMemcpyAsync(keys_out, keys_in, n * W * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+        identity_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(vals_in, vals_out, n);
+        QMBX_LAUNCH_CHECK("identity_kernel");
+        return QMBX_OK;
+    }
+    const uint64_t* src_k = keys_in;
+    const int32_t* src_v = vals_in;
+    for (int p = 0; p < n_bytes; ++p) {
+        int b = n_bytes - 1 - p;  // row byte handled by this pass, least significant first
+        int word = b >> 3;
+        int shift = 8 * (7 - (b & 7));
+        bool to_out = ((n_bytes - 1 - p) & 1) == 0;
+        uint64_t* dst_k = to_out ? keys_out : sc.keys;
+        int32_t* dst_v = to_out ? vals_out : sc.vals;
+        radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks);
+        int st = exclusive_scan(sc.counts, sc.counts, (int64_t)256 * nblocks, nullptr, sc.scan, s);
+        if (st != QMBX_OK) return st;
+        radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
+                                                                 nblocks);
+        QMBX_LAUNCH_CHECK("radix sort pass");
+        src_k = dst_k;
+        src_v = dst_v;
+    }
+    return QMBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sorted, de-duplicated row sets
+// ---------------------------------------------------------------------------
+
+template <int W>
+__global__ void head_flags_kernel(const uint64_t* __restrict__ sorted, int64_t n, int32_t* __restrict__ head) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t h = 1;
+    if (i > 0) {
+        Key<W> a = load_key<W>(sorted, i - 1);
+        Key<W> b = load_key<W>(sorted, i);
+        h = key_eq<W>(a, b) ? 0 : 1;
+    }
+    head[i] = h;
+}
+
+template <int W>
+__global__ void compact_heads_kernel(const uint64_t* __restrict__ sorted, const int32_t* __restrict__ perm,
+                                     const int32_t* __restrict__ head, const int32_t* __restrict__ pos, int64_t n,
+                                     uint64_t* __restrict__ ukeys, int32_t* __restrict__ first,
+                                     int32_t* __restrict__ start, int* __restrict__ count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (head[i]) {
+        int32_t u = pos[i];
+        store_key<W>(ukeys, u, load_key<W>(sorted, i));
+        first[u] = perm[i];
+        start[u] = (int32_t)i;
+    }
+    if (i == n - 1) {
+        int32_t total = pos[i] + head[i];
+        *count = total;
+        start[total] = (int32_t)n;
+    }
+}
+
+
+
+template <int W>
+RowSet take_rowset(Arena& ws, int64_t n) {
+    RowSet out;
+    uint64_t cap = (uint64_t)(n > 0 ? n : 1);
+    out.n = n;
+    out.packed = ws.take<uint64_t>(cap * W);
+    out.sorted_keys = ws.take<uint64_t>(cap * W);
+    out.perm = ws.take<int32_t>(cap);
+    out.keys = ws.take<uint64_t>(cap * W);
+    out.first = ws.take<int32_t>(cap);
+    out.start = ws.take<int32_t>(cap + 1);
+    out.count = ws.take<int>(1);
+    out.head = ws.take<int32_t>(cap);
+    out.pos = ws.take<int32_t>(cap);
+    out.sort = take_sort_scratch<W>(ws, n);
+    return out;
+}
+
+template <int W>
+int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
+    const int64_t n = out.n;
+    if (n == 0) {
+        set_int_kernel<<<1, 1, 0, s>>>(out.count, 0);
+        QMBX_LAUNCH_CHECK("set_int_kernel");
+        return QMBX_OK;
+    }
+    int st;
+    if ((st = pack_rows<W>(rows, n, nq, out.packed, s)) != QMBX_OK) return st;
+    if ((st = sort_pairs<W>(out.packed, nullptr, out.sorted_keys, out.perm, n, nq, out.sort, s)) != QMBX_OK) return st;
+    head_flags_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, n, out.head);
+    if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.sort.scan, s)) != QMBX_OK) return st;
+    compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
+                                                                       out.keys, out.first, out.start, out.count);
+    QMBX_LAUNCH_CHECK("build_rowset");
+    return QMBX_OK;
+}
+
+#define QMBX_INSTANTIATE_KEYS(W)                                                                                \
+    template int pack_rows<W>(const uint8_t*, int64_t, int, uint64_t*, cudaStream_t);                           \
+    template int unpack_rows<W>(const uint64_t*, const int*, int64_t, int, uint8_t*, cudaStream_t);             \
+    template SortScratch take_sort_scratch<W>(Arena&, int64_t);                                                 \
+    template int sort_pairs<W>(const uint64_t*, const int32_t*, uint64_t*, int32_t*, int64_t, int,              \
+                               const SortScratch&, cudaStream_t);                                               \
+    template RowSet take_rowset<W>(Arena&, int64_t);                                                            \
+    template int build_rowset<W>(const uint8_t*, int, RowSet&, cudaStream_t);
+
+QMBX_INSTANTIATE_KEYS(1)
+QMBX_INSTANTIATE_KEYS(2)
+QMBX_INSTANTIATE_KEYS(3)
+QMBX_INSTANTIATE_KEYS(4)
+
+}  // namespace qmbx

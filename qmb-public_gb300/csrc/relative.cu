@@ -1,0 +1,527 @@
+// find_relative and single_relative.
+//
+// The reference keeps a global min-heap of count_selected records guarded by
+// per-node spin locks (qmb/_hamiltonian_cuda.cu:276-675) and samples
+// single_relative neighbours under per-row locks (:805-996).  Here neither
+// needs a lock or any device-side wait:
+//
+//   find_relative  pass 1 counts the candidate records per weight bucket (the
+//                  top 12 bits of an FP32 estimate |coef|^2 |psi|^2 of the
+//                  weight); the host picks the bucket that holds the
+//                  count_selected-th record; pass 2 re-enumerates and keeps
+//                  only records at or above the bucket below it, now with the
+//                  exact FP64 weight of the reference (:494-497); a radix
+//                  sort ranks them by (weight, visiting order) and the first
+//                  count_selected are sorted and de-duplicated by row.
+//   single_relative  one thread per row keeps the best Efraimidis-Spirakis
+//                  key of its candidates in registers.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "device.cuh"
+
+namespace qmbx {
+namespace {
+
+constexpr int kBuckets = 4096;
+
+__device__ __forceinline__ int weight_bucket(float est) {
+    // 0 for zero (or underflowed) estimates; otherwise 1 + the top 12 bits of
+    // the IEEE pattern, which is monotone for non-negative floats
+    return est > 0.f ? 1 + (int)(__float_as_uint(est) >> 20) : 0;
+}
+
+// The reference's weight (qmb/_hamiltonian_cuda.cu:494-497), every product
+// and sum rounded once in that order.
+__device__ __forceinline__ double exact_weight(double2 cf, double2 p, int parity) {
+    double re = __dsub_rn(__dmul_rn(cf.x, p.x), __dmul_rn(cf.y, p.y));
+    double im = __dadd_rn(__dmul_rn(cf.x, p.y), __dmul_rn(cf.y, p.x));
+    if (parity) {
+        re = -re;
+        im = -im;
+    }
+    return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+}
+
+// The histogram and emission passes need per-row data (|psi|^2) and a shared
+// histogram, so they use their own kernel rather than enumerate_kernel.
+struct RelativeArgs {
+    const uint64_t* keys_i;  // packed configs_i, input order
+    const double2* psi;
+    int64_t n_i;
+    const uint64_t* excl;    // sorted unique exclude keys
+    const int* n_excl;
+    PartView off, diag;
+    // pass 1
+    unsigned long long* hist;
+    // pass 2
+    int emit_from;           // lowest bucket emitted
+    unsigned long long* n_emit;
+    int64_t cap_emit;
+    uint64_t* emit_rank;     // [cap][2]: ~weight bits, ~order
+    uint64_t* emit_keys;     // [cap][W]
+    int* overflow;
+};
+
+template <int W, bool EMIT>
+__device__ __forceinline__ void relative_candidate(const RelativeArgs& a, int* s_hist, const Key<W>& img, float norm,
+                                                   float m, double2 cf, double2 p, int parity, int64_t orig,
+                                                   int64_t row, int64_t n_ex) {
+    if (find_key<W>(a.excl, n_ex, img) >= 0) return;
+    int b = weight_bucket(__fmul_rn(norm, m));
+    if (!EMIT) {
+        atomicAdd(&s_hist[b], 1);
+        return;
+    }
+    if (b < a.emit_from) return;
+    double w = exact_weight(cf, p, parity);
+    if (w == 0.0) return;
+    unsigned long long slot = atomicAdd(a.n_emit, 1ull);
+    if ((int64_t)slot >= a.cap_emit) {
+        *a.overflow = 1;
+        return;
+    }
+    uint64_t order = (uint64_t)orig * (uint64_t)a.n_i + (uint64_t)row;
+    a.emit_rank[2 * slot + 0] = ~(uint64_t)__double_as_longlong(w);
+    a.emit_rank[2 * slot + 1] = ~order;
+#pragma unroll
+    for (int q = 0; q < W; ++q) a.emit_keys[slot * W + q] = img.w[q];
+}
+
+template <int W, bool EMIT>
+__global__ void __launch_bounds__(kThreads) relative_kernel(RelativeArgs a) {
+    __shared__ TermTile<W> tile;
+    __shared__ int s_hist[EMIT ? 1 : kBuckets];
+    if (!EMIT) {
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) s_hist[k] = 0;
+    }
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = row < a.n_i;
+    Key<W> c;
+    double2 p = make_double2(0.0, 0.0);
+    if (live) {
+        c = load_key<W>(a.keys_i, row);
+        p = a.psi[row];
+    } else {
+#pragma unroll
+        for (int q = 0; q < W; ++q) c.w[q] = 0;
+    }
+    const float m = (float)(p.x * p.x + p.y * p.y);
+    const int64_t n_ex = *a.n_excl;
+    for (int part = 0; part < 2; ++part) {
+        const PartView& pv = part == 0 ? a.off : a.diag;
+        for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
+            int count = (int)(pv.n - t0 < kTermTile ? pv.n - t0 : kTermTile);
+            __syncthreads();
+            stage_tile<W>(tile, pv, t0, count);
+            __syncthreads();
+            if (live) {
+                for (int k = 0; k < count; ++k) {
+                    const uint64_t* t = tile.m[k];
+                    if (term_applies<W>(t, c)) {
+                        Key<W> img;
+                        int parity = term_image<W>(t, c, img);
+                        int64_t slot = t0 + k;
+                        double2 cf = EMIT ? __ldg(pv.coef + slot) : make_double2(0.0, 0.0);
+                        int64_t orig = EMIT ? __ldg(pv.orig + slot) : 0;
+                        relative_candidate<W, EMIT>(a, s_hist, img, __ldg(pv.norm + slot), m, cf, p, parity, orig,
+                                                    row, n_ex);
+                    }
+                }
+            }
+        }
+    }
+    if (!EMIT) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
+            int v = s_hist[k];
+            if (v) atomicAdd(a.hist + k, (unsigned long long)v);
+        }
+    }
+}
+
+// Gather the keys of the first `keep` ranked records.
+template <int W>
+__global__ void gather_selected_kernel(const int32_t* __restrict__ order, const uint64_t* __restrict__ keys,
+                                       int64_t keep, uint64_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= keep) return;
+    int64_t src = order[i];
+#pragma unroll
+    for (int q = 0; q < W; ++q) out[i * W + q] = keys[src * W + q];
+}
+
+__global__ void zero_u64_kernel(unsigned long long* p, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 0;
+}
+
+struct FindArgs {
+    const void* table_host;
+    const void* table_dev;
+    const uint8_t* configs_i;
+    const double* psi_i;
+    int64_t n_i;
+    int64_t k;
+    const uint8_t* configs_ex;
+    int64_t n_ex;
+    uint8_t* out;
+    int64_t* n_out;
+};
+
+// Workspace layout: fixed part (exclude set, packed rows, histogram, flags,
+// final row set of up to k rows), then the emission area of cap records.
+template <int W>
+struct FindLayout {
+    RowSet excl;
+    uint64_t* keys_i;
+    unsigned long long* hist;
+    unsigned long long* n_emit;
+    int* overflow;
+    uint64_t* sel_keys;
+    RowSet final_set;  // built from sel_keys through a second rowset (rows are keys here)
+    // emission area
+    uint64_t* emit_rank;
+    uint64_t* emit_keys;
+    int32_t* rank_order;
+    uint64_t* rank_sorted;
+    SortScratch rank_sort;
+};
+
+template <int W>
+uint64_t record_bytes() {
+    // rank key (16 B) + image key (8W) + sorted copy (16 B) + order (4 B) + sort scratch (16 + 4 B), rounded up
+    return 16 + 8 * W + 16 + 4 + 16 + 4 + 8;
+}
+
+template <int W>
+FindLayout<W> take_find(Arena& ws, int64_t n_i, int64_t k, int64_t n_ex, int64_t cap) {
+    FindLayout<W> L;
+    L.excl = take_rowset<W>(ws, n_ex);
+    L.keys_i = ws.take<uint64_t>((uint64_t)(n_i > 0 ? n_i : 1) * W);
+    L.hist = ws.take<unsigned long long>(kBuckets + 1);
+    L.n_emit = L.hist + kBuckets;
+    L.overflow = ws.take<int>(1);
+    int64_t kk = k > 0 ? k : 1;
+    L.sel_keys = ws.take<uint64_t>((uint64_t)kk * W);
+    L.final_set = take_rowset<W>(ws, kk);
+    int64_t c = cap > 0 ? cap : 1;
+    L.emit_rank = ws.take<uint64_t>((uint64_t)c * 2);
+    L.emit_keys = ws.take<uint64_t>((uint64_t)c * W);
+    L.rank_order = ws.take<int32_t>((uint64_t)c);
+    L.rank_sorted = ws.take<uint64_t>((uint64_t)c * 2);
+    L.rank_sort = take_sort_scratch<2>(ws, c);
+    return L;
+}
+
+template <int W>
+int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint64_t* needed, cudaStream_t s) {
+    const qmbx_table_header* h = header_of(a.table_host);
+    const int nq = h->n_qubytes;
+    const int64_t k = a.k;
+    // initial emission capacity: what the workspace can hold
+    Arena probe(nullptr, 0);
+    take_find<W>(probe, a.n_i, k, a.n_ex, 1);
+    uint64_t fixed = probe.used;
+    int64_t cap = 1;
+    if (workspace_bytes > fixed) cap = (int64_t)((workspace_bytes - fixed) / (2 * record_bytes<W>())) + 1;
+    for (;;) {
+        Arena trial(nullptr, 0);
+        take_find<W>(trial, a.n_i, k, a.n_ex, cap);
+        if (trial.used <= workspace_bytes || cap == 1) break;
+        cap = cap * 3 / 4;
+        if (cap < 1) cap = 1;
+    }
+    Arena ws(workspace, workspace_bytes);
+    FindLayout<W> L = take_find<W>(ws, a.n_i, k, a.n_ex, cap);
+    if (workspace == nullptr || !ws.fits()) {
+        if (needed) *needed = ws.used;
+        return fail(QMBX_ERR_WORKSPACE, "find_relative needs at least %llu bytes of workspace",
+                    (unsigned long long)ws.used);
+    }
+    *a.n_out = 0;
+    if (k == 0 || a.n_i == 0) return QMBX_OK;
+    int st;
+    if ((st = build_rowset<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
+    if ((st = pack_rows<W>(a.configs_i, a.n_i, nq, L.keys_i, s)) != QMBX_OK) return st;
+    zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1);
+    QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
+
+    RelativeArgs r{};
+    r.keys_i = L.keys_i;
+    r.psi = reinterpret_cast<const double2*>(a.psi_i);
+    r.n_i = a.n_i;
+    r.excl = L.excl.keys;
+    r.n_excl = L.excl.count;
+    r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
+    r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
+    r.hist = L.hist;
+    const unsigned grid = grid_for(a.n_i, kThreads);
+    relative_kernel<W, false><<<grid, kThreads, 0, s>>>(r);
+    QMBX_LAUNCH_CHECK("find_relative histogram pass");
+
+    std::vector<unsigned long long> hist(kBuckets);
+    QMBX_CUDA_TRY(cudaMemcpyAsync(hist.data(), L.hist, kBuckets * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    // bucket holding the k-th heaviest record (records with a zero estimate
+    // sit in bucket 0 and are emitted only when fewer than k records lie above)
+    unsigned long long above = 0;
+    int b_k = 0;
+    for (int b = kBuckets - 1; b >= 1; --b) {
+        above += hist[b];
+        if (above >= (unsigned long long)k) {
+            b_k = b;
+            break;
+        }
+    }
+    int emit_from = b_k > 1 ? b_k - 1 : 0;
+    unsigned long long need = 0;
+    for (int b = emit_from; b < kBuckets; ++b) need += hist[b];
+    if ((int64_t)need > cap) {
+        Arena want(nullptr, 0);
+        take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)need);
+        if (needed) *needed = want.used;
+        return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
+                    (unsigned long long)want.used, need);
+    }
+    if (need == 0) return QMBX_OK;
+    r.emit_from = emit_from;
+    r.n_emit = L.n_emit;
+    r.cap_emit = cap;
+    r.emit_rank = L.emit_rank;
+    r.emit_keys = L.emit_keys;
+    r.overflow = L.overflow;
+    relative_kernel<W, true><<<grid, kThreads, 0, s>>>(r);
+    QMBX_LAUNCH_CHECK("find_relative emission pass");
+    unsigned long long n_emit = 0;
+    int overflow = 0;
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&overflow, L.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    if (overflow || (int64_t)n_emit > cap) {
+        return fail(QMBX_ERR_DEVICE, "find_relative emitted %llu records into room for %lld", n_emit, (long long)cap);
+    }
+    if (n_emit == 0) return QMBX_OK;
+    const int64_t e = (int64_t)n_emit;
+    if ((st = sort_pairs<2>(L.emit_rank, nullptr, L.rank_sorted, L.rank_order, e, 16, L.rank_sort, s)) != QMBX_OK) {
+        return st;
+    }
+    const int64_t keep = e < k ? e : k;
+    gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
+                                                                            L.sel_keys);
+    QMBX_LAUNCH_CHECK("gather_selected_kernel");
+    // sort and de-duplicate the selected rows: unpack to bytes in the output
+    // buffer, then build a row set from those bytes
+    if ((st = unpack_rows<W>(L.sel_keys, nullptr, keep, nq, a.out, s)) != QMBX_OK) return st;
+    L.final_set.n = keep;
+    if ((st = build_rowset<W>(a.out, nq, L.final_set, s)) != QMBX_OK) return st;
+    int n_unique = 0;
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_unique, L.final_set.count, sizeof(int), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    if ((st = unpack_rows<W>(L.final_set.keys, nullptr, n_unique, nq, a.out, s)) != QMBX_OK) return st;
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    *a.n_out = n_unique;
+    return QMBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single_relative
+// ---------------------------------------------------------------------------
+
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// key factor log(u_t) / |coef_t| of every changing term (-inf for zero coefficients)
+__global__ void es_factor_kernel(const double2* __restrict__ coef, const int32_t* __restrict__ orig, int64_t n,
+                                 uint64_t seed, double* __restrict__ kf) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 c = coef[i];
+    double w = sqrt(c.x * c.x + c.y * c.y);
+    uint64_t bits = splitmix64(seed ^ splitmix64((uint64_t)orig[i]));
+    double u = (double)((bits >> 11) + 1) * (1.0 / 9007199254740992.0);
+    kf[i] = w > 0.0 ? log(u) / w : -INFINITY;
+}
+
+template <int W>
+struct SingleVisitor {
+    const uint64_t* set;
+    const int* n_set;
+    const double* kf;
+    const int32_t* orig;
+    uint8_t* out;
+    int nq;
+    struct Acc {
+        double key;
+        int32_t term;
+        Key<W> best;
+        int64_t n;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
+        a.key = -INFINITY;
+        a.term = -1;
+        a.n = *n_set;
+#pragma unroll
+        for (int q = 0; q < W; ++q) a.best.w[q] = 0;
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int, int64_t slot) const {
+        double key = __ldg(kf + slot);
+        int32_t t = __ldg(orig + slot);
+        bool better = a.term < 0 || key > a.key || (key == a.key && t < a.term);
+        if (!better) return;
+        if (find_key<W>(set, a.n, img) >= 0) return;
+        a.key = key;
+        a.term = t;
+        a.best = img;
+    }
+    __device__ __forceinline__ void visit_diag(Acc&, const Key<W>&, int, int64_t) const {}
+    __device__ __forceinline__ void finish(Acc& a, int64_t row, const Key<W>&) const {
+        uint8_t* r = out + row * nq;
+        for (int b = 0; b < nq; ++b) r[b] = (uint8_t)(a.best.w[b >> 3] >> (8 * (7 - (b & 7))));
+    }
+};
+
+template <int W>
+struct SingleLayout {
+    RowSet set;
+    double* kf;
+};
+
+template <int W>
+SingleLayout<W> take_single(Arena& ws, int64_t n, int64_t n_off) {
+    SingleLayout<W> L;
+    L.set = take_rowset<W>(ws, n);
+    L.kf = ws.take<double>((uint64_t)(n_off > 0 ? n_off : 1));
+    return L;
+}
+
+template <int W>
+int single_impl(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n, uint64_t seed,
+                uint8_t* out, Arena& ws, cudaStream_t s) {
+    const qmbx_table_header* h = header_of(table_host);
+    PartView off = part_view(table_host, table_dev, QMBX_PART_FWD);
+    SingleLayout<W> L = take_single<W>(ws, n, h->part[QMBX_PART_FWD].n);
+    if (ws.base == nullptr) return QMBX_OK;
+    if (!ws.fits()) return fail(QMBX_ERR_WORKSPACE, "single_relative needs %llu bytes of workspace", (unsigned long long)ws.used);
+    if (n == 0) return QMBX_OK;
+    int st;
+    if ((st = build_rowset<W>(configs, h->n_qubytes, L.set, s)) != QMBX_OK) return st;
+    if (off.n > 0) {
+        es_factor_kernel<<<grid_for(off.n, kThreads), kThreads, 0, s>>>(off.coef, off.orig, off.n, seed, L.kf);
+        QMBX_LAUNCH_CHECK("es_factor_kernel");
+    }
+    PartView none = off;
+    none.n = 0;
+    SingleVisitor<W> v{L.set.keys, L.set.count, L.kf, off.orig, out, h->n_qubytes};
+    KeyRows<W> src{L.set.packed};
+    enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none);
+    QMBX_LAUNCH_CHECK("single_relative enumeration");
+    return QMBX_OK;
+}
+
+int check_ws(void* workspace) {
+    if (workspace != nullptr && reinterpret_cast<uintptr_t>(workspace) % QMBX_ALIGN != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "workspace must be %d-byte aligned", QMBX_ALIGN);
+    }
+    return QMBX_OK;
+}
+
+}  // namespace
+}  // namespace qmbx
+
+using namespace qmbx;
+
+extern "C" int qmbx_find_relative_workspace(const void* table_host, int64_t n_i, int64_t count_selected,
+                                            int64_t n_exclude, uint64_t* bytes) {
+    clear_error();
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    int64_t k = count_selected > 0 ? count_selected : 0;
+    int64_t cap = 4 * k + (1 << 16);
+    Arena probe(nullptr, 0);
+    switch (h->n_words) {
+        case 1: take_find<1>(probe, n_i, k, n_exclude, cap); break;
+        case 2: take_find<2>(probe, n_i, k, n_exclude, cap); break;
+        case 3: take_find<3>(probe, n_i, k, n_exclude, cap); break;
+        case 4: take_find<4>(probe, n_i, k, n_exclude, cap); break;
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+    *bytes = probe.used;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_find_relative(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                  const double* psi_i, int64_t n_i, int64_t count_selected,
+                                  const uint8_t* configs_exclude, int64_t n_exclude, uint8_t* out, int64_t* n_out,
+                                  void* workspace, uint64_t workspace_bytes, uint64_t* workspace_needed,
+                                  qmbx_stream_t stream) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if (n_out == nullptr) return fail(QMBX_ERR_ARGUMENT, "n_out must not be NULL");
+    if (count_selected < 0) return fail(QMBX_ERR_ARGUMENT, "count_selected must not be negative");
+    if (count_selected >= (int64_t(1) << 31)) return fail(QMBX_ERR_ARGUMENT, "count_selected too large");
+    if (n_i < 0 || n_i >= (int64_t(1) << 31) || n_exclude < 0 || n_exclude >= (int64_t(1) << 31)) {
+        return fail(QMBX_ERR_ARGUMENT, "row count out of range");
+    }
+    if ((n_i > 0 && (configs_i == nullptr || psi_i == nullptr)) || (n_exclude > 0 && configs_exclude == nullptr)) {
+        return fail(QMBX_ERR_ARGUMENT, "input pointers must not be NULL");
+    }
+    if (count_selected > 0 && out == nullptr) return fail(QMBX_ERR_ARGUMENT, "out must not be NULL");
+    if ((st = check_ws(workspace)) != QMBX_OK) return st;
+    if (workspace == nullptr) workspace_bytes = 0;
+    FindArgs a{table_host, table_dev, configs_i, psi_i, n_i, count_selected, configs_exclude, n_exclude, out, n_out};
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    switch (header_of(table_host)->n_words) {
+        case 1: return find_impl<1>(a, workspace, workspace_bytes, workspace_needed, s);
+        case 2: return find_impl<2>(a, workspace, workspace_bytes, workspace_needed, s);
+        case 3: return find_impl<3>(a, workspace, workspace_bytes, workspace_needed, s);
+        case 4: return find_impl<4>(a, workspace, workspace_bytes, workspace_needed, s);
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+}
+
+extern "C" int qmbx_single_relative_workspace(const void* table_host, int64_t n, uint64_t* bytes) {
+    clear_error();
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    Arena probe(nullptr, 0);
+    int64_t n_off = h->part[QMBX_PART_FWD].n;
+    switch (h->n_words) {
+        case 1: take_single<1>(probe, n, n_off); break;
+        case 2: take_single<2>(probe, n, n_off); break;
+        case 3: take_single<3>(probe, n, n_off); break;
+        case 4: take_single<4>(probe, n, n_off); break;
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+    *bytes = probe.used;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_single_relative(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n,
+                                    uint64_t seed, uint8_t* out, void* workspace, uint64_t workspace_bytes,
+                                    qmbx_stream_t stream) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if (n < 0 || n >= (int64_t(1) << 31)) return fail(QMBX_ERR_ARGUMENT, "row count out of range");
+    if (n > 0 && (configs == nullptr || out == nullptr)) return fail(QMBX_ERR_ARGUMENT, "pointers must not be NULL");
+    if ((st = check_ws(workspace)) != QMBX_OK) return st;
+    if (workspace == nullptr) return fail(QMBX_ERR_WORKSPACE, "single_relative needs a workspace");
+    Arena ws(workspace, workspace_bytes);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    switch (header_of(table_host)->n_words) {
+        case 1: return single_impl<1>(table_host, table_dev, configs, n, seed, out, ws, s);
+        case 2: return single_impl<2>(table_host, table_dev, configs, n, seed, out, ws, s);
+        case 3: return single_impl<3>(table_host, table_dev, configs, n, seed, out, ws, s);
+        case 4: return single_impl<4>(table_host, table_dev, configs, n, seed, out, ws, s);
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+}

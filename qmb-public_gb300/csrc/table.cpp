@@ -1,0 +1,290 @@
+// Host-side term compiler and error plumbing of the qmbx C ABI.
+//
+// qmbx_table_build replaces the per-call, per-thread decoding of
+// (site, kind) slots that the reference performs inside every kernel thread
+// (qmb/_hamiltonian_cuda.cu:54-84) with a one-off compilation into bit masks
+// (see format.h for the closed form).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qmbx.h"
+#include "common.h"
+#include "format.h"
+
+namespace qmbx {
+
+static thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+namespace {
+
+struct Compiled {
+    bool live = true;
+    uint64_t mask[QMBX_MAX_WORDS] = {0, 0, 0, 0};
+    uint64_t val[QMBX_MAX_WORDS] = {0, 0, 0, 0};
+    uint64_t flip[QMBX_MAX_WORDS] = {0, 0, 0, 0};
+    uint64_t par[QMBX_MAX_WORDS] = {0, 0, 0, 0};
+    int pconst = 0;
+    bool diagonal() const { return (flip[0] | flip[1] | flip[2] | flip[3]) == 0; }
+};
+
+struct Below {
+    // below[s] = key-space mask of every site < s
+    std::vector<uint64_t> m;
+    int words;
+    Below(int n_sites, int w) : m((size_t)(n_sites + 1) * QMBX_MAX_WORDS, 0), words(w) {
+        for (int s = 1; s <= n_sites; ++s) {
+            uint64_t* row = &m[(size_t)s * QMBX_MAX_WORDS];
+            const uint64_t* prev = &m[(size_t)(s - 1) * QMBX_MAX_WORDS];
+            for (int k = 0; k < QMBX_MAX_WORDS; ++k) row[k] = prev[k];
+            row[qmbx_keyword(s - 1)] |= 1ull << qmbx_keybit(s - 1);
+        }
+    }
+    const uint64_t* of(int s) const { return &m[(size_t)s * QMBX_MAX_WORDS]; }
+};
+
+int parity64(uint64_t x) { return __builtin_popcountll(x) & 1; }
+
+// Replay the slots from the last to the first (qmb/_hamiltonian_cpu.cpp:59-76)
+// symbolically.  adjoint = true compiles the daggered term: slots in reverse
+// order with create and annihilate exchanged.
+Compiled compile_term(const int16_t* site, const uint8_t* kind, bool fermi, bool adjoint, const Below& below) {
+    Compiled c;
+    uint64_t known[QMBX_MAX_WORDS] = {0, 0, 0, 0};
+    uint64_t now[QMBX_MAX_WORDS] = {0, 0, 0, 0};  // current value of known sites
+    for (int step = 0; step < 4; ++step) {
+        int slot = adjoint ? step : 3 - step;
+        int k = kind[slot];
+        if (k == 2) continue;
+        if (adjoint) k = 1 - k;
+        int s = site[slot];
+        int w = qmbx_keyword(s);
+        uint64_t bit = 1ull << qmbx_keybit(s);
+        if (!(known[w] & bit)) {
+            known[w] |= bit;
+            c.mask[w] |= bit;
+            if (k == 0) {  // annihilation needs the site occupied
+                c.val[w] |= bit;
+                now[w] |= bit;
+            }
+        }
+        int current = (now[w] & bit) ? 1 : 0;
+        if (current == k) {
+            c.live = false;
+            return c;
+        }
+        now[w] ^= bit;
+        c.flip[w] ^= bit;
+        if (fermi) {
+            const uint64_t* b = below.of(s);
+            for (int q = 0; q < QMBX_MAX_WORDS; ++q) {
+                c.par[q] ^= b[q];
+                c.pconst ^= parity64(c.flip[q] & b[q]);
+            }
+        }
+    }
+    return c;
+}
+
+uint64_t align_up(uint64_t x) { return (x + QMBX_ALIGN - 1) / QMBX_ALIGN * QMBX_ALIGN; }
+
+int validate(const int16_t* site, const uint8_t* kind, int64_t n_terms, int32_t n_qubytes, int32_t particle_cut) {
+    if (n_qubytes < 1 || n_qubytes > 8 * QMBX_MAX_WORDS) {
+        return fail(QMBX_ERR_ARGUMENT, "n_qubytes must be in [1, %d], got %d", 8 * QMBX_MAX_WORDS, n_qubytes);
+    }
+    if (particle_cut != 1 && particle_cut != 2) {
+        return fail(QMBX_ERR_ARGUMENT, "particle_cut must be 1 (fermi) or 2 (bose2), got %d", particle_cut);
+    }
+    if (n_terms < 0 || n_terms >= (int64_t(1) << 31)) {
+        return fail(QMBX_ERR_ARGUMENT, "term count out of range: %lld", (long long)n_terms);
+    }
+    if (n_terms > 0 && (site == nullptr || kind == nullptr)) {
+        return fail(QMBX_ERR_ARGUMENT, "site and kind must not be NULL");
+    }
+    int n_sites = 8 * n_qubytes;
+    for (int64_t t = 0; t < n_terms; ++t) {
+        for (int k = 0; k < 4; ++k) {
+            int kd = kind[t * 4 + k];
+            if (kd > 2) {
+                return fail(QMBX_ERR_ARGUMENT, "term %lld slot %d: kind must be 0, 1 or 2, got %d", (long long)t, k, kd);
+            }
+            if (kd != 2) {
+                int s = site[t * 4 + k];
+                if (s < 0 || s >= n_sites) {
+                    return fail(QMBX_ERR_ARGUMENT, "term %lld slot %d: site %d outside [0, %d)", (long long)t, k, s,
+                                n_sites);
+                }
+            }
+        }
+    }
+    return QMBX_OK;
+}
+
+struct Layout {
+    qmbx_table_header h;
+};
+
+void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
+    p.n = n;
+    uint64_t un = (uint64_t)n;
+    p.off_test = cursor;
+    cursor = align_up(cursor + un * 2 * words * 8);
+    p.off_apply = cursor;
+    cursor = align_up(cursor + un * 2 * words * 8);
+    p.off_coef = cursor;
+    cursor = align_up(cursor + un * 16);
+    p.off_coef32 = cursor;
+    cursor = align_up(cursor + un * 16);
+    p.off_orig = cursor;
+    cursor = align_up(cursor + un * 4);
+    p.off_norm = cursor;
+    cursor = align_up(cursor + un * 4);
+}
+
+qmbx_table_header make_header(int64_t n_terms, int32_t n_qubytes, int32_t particle_cut, int64_t n_off, int64_t n_diag) {
+    qmbx_table_header h;
+    std::memset(&h, 0, sizeof(h));
+    h.magic = QMBX_MAGIC;
+    h.version = QMBX_TABLE_VERSION;
+    h.n_qubytes = n_qubytes;
+    h.particle_cut = particle_cut;
+    h.n_words = (n_qubytes + 7) / 8;
+    h.n_sites = 8 * n_qubytes;
+    h.n_terms = n_terms;
+    h.n_live = n_off + n_diag;
+    uint64_t cursor = align_up(sizeof(qmbx_table_header));
+    layout_part(h.part[QMBX_PART_FWD], n_off, h.n_words, cursor);
+    layout_part(h.part[QMBX_PART_ADJ], n_off, h.n_words, cursor);
+    layout_part(h.part[QMBX_PART_DIAG], n_diag, h.n_words, cursor);
+    h.total_bytes = cursor;
+    return h;
+}
+
+void count_terms(const int16_t* site, const uint8_t* kind, int64_t n_terms, int32_t n_qubytes, int32_t particle_cut,
+                 int64_t& n_off, int64_t& n_diag) {
+    Below below(8 * n_qubytes, (n_qubytes + 7) / 8);
+    n_off = n_diag = 0;
+    for (int64_t t = 0; t < n_terms; ++t) {
+        Compiled c = compile_term(site + 4 * t, kind + 4 * t, particle_cut == 1, false, below);
+        if (!c.live) continue;
+        if (c.diagonal()) {
+            ++n_diag;
+        } else {
+            ++n_off;
+        }
+    }
+}
+
+void write_term(char* blob, const qmbx_table_part& p, int words, int64_t slot, const Compiled& c, const double* coef,
+                int64_t orig) {
+    uint64_t* test = reinterpret_cast<uint64_t*>(blob + p.off_test) + slot * 2 * words;
+    uint64_t* apply = reinterpret_cast<uint64_t*>(blob + p.off_apply) + slot * 2 * words;
+    for (int w = 0; w < words; ++w) {
+        test[2 * w + 0] = c.mask[w];
+        test[2 * w + 1] = c.val[w];
+        apply[2 * w + 0] = c.flip[w];
+        apply[2 * w + 1] = c.par[w];
+    }
+    double re = coef[0], im = coef[1];
+    if (c.pconst) {
+        re = -re;
+        im = -im;
+    }
+    double* cf = reinterpret_cast<double*>(blob + p.off_coef) + slot * 2;
+    cf[0] = re;
+    cf[1] = im;
+    float* c32 = reinterpret_cast<float*>(blob + p.off_coef32) + slot * 4;
+    float re_hi = (float)re, im_hi = (float)im;
+    c32[0] = re_hi;
+    c32[1] = (float)(re - (double)re_hi);
+    c32[2] = im_hi;
+    c32[3] = (float)(im - (double)im_hi);
+    reinterpret_cast<int32_t*>(blob + p.off_orig)[slot] = (int32_t)orig;
+    reinterpret_cast<float*>(blob + p.off_norm)[slot] = (float)(re * re + im * im);
+}
+
+}  // namespace
+}  // namespace qmbx
+
+using namespace qmbx;
+
+extern "C" int qmbx_version(void) { return 10000; }
+
+extern "C" const char* qmbx_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int qmbx_table_bytes(const int16_t* site, const uint8_t* kind, int64_t n_terms, int32_t n_qubytes,
+                                int32_t particle_cut, uint64_t* bytes) {
+    clear_error();
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    int st = validate(site, kind, n_terms, n_qubytes, particle_cut);
+    if (st != QMBX_OK) return st;
+    int64_t n_off, n_diag;
+    count_terms(site, kind, n_terms, n_qubytes, particle_cut, n_off, n_diag);
+    *bytes = make_header(n_terms, n_qubytes, particle_cut, n_off, n_diag).total_bytes;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_table_build(const int16_t* site, const uint8_t* kind, const double* coef, int64_t n_terms,
+                                int32_t n_qubytes, int32_t particle_cut, void* blob, uint64_t blob_bytes) {
+    clear_error();
+    int st = validate(site, kind, n_terms, n_qubytes, particle_cut);
+    if (st != QMBX_OK) return st;
+    if (n_terms > 0 && coef == nullptr) return fail(QMBX_ERR_ARGUMENT, "coef must not be NULL");
+    if (blob == nullptr) return fail(QMBX_ERR_ARGUMENT, "blob must not be NULL");
+    int64_t n_off, n_diag;
+    count_terms(site, kind, n_terms, n_qubytes, particle_cut, n_off, n_diag);
+    qmbx_table_header h = make_header(n_terms, n_qubytes, particle_cut, n_off, n_diag);
+    if (blob_bytes < h.total_bytes) {
+        return fail(QMBX_ERR_ARGUMENT, "table blob holds %llu bytes, needs %llu", (unsigned long long)blob_bytes,
+                    (unsigned long long)h.total_bytes);
+    }
+    char* out = static_cast<char*>(blob);
+    std::memset(out, 0, h.total_bytes);
+    std::memcpy(out, &h, sizeof(h));
+    Below below(h.n_sites, h.n_words);
+    bool fermi = particle_cut == 1;
+    int64_t k_off = 0, k_diag = 0;
+    for (int64_t t = 0; t < n_terms; ++t) {
+        Compiled c = compile_term(site + 4 * t, kind + 4 * t, fermi, false, below);
+        if (!c.live) continue;
+        if (c.diagonal()) {
+            write_term(out, h.part[QMBX_PART_DIAG], h.n_words, k_diag++, c, coef + 2 * t, t);
+        } else {
+            write_term(out, h.part[QMBX_PART_FWD], h.n_words, k_off, c, coef + 2 * t, t);
+            Compiled a = compile_term(site + 4 * t, kind + 4 * t, fermi, true, below);
+            write_term(out, h.part[QMBX_PART_ADJ], h.n_words, k_off, a, coef + 2 * t, t);
+            ++k_off;
+        }
+    }
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_table_counts(const void* table_host, int64_t counts[6]) {
+    clear_error();
+    const qmbx_table_header* h = static_cast<const qmbx_table_header*>(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC || h->version != QMBX_TABLE_VERSION) {
+        return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    }
+    counts[0] = h->n_terms;
+    counts[1] = h->n_live;
+    counts[2] = h->part[QMBX_PART_DIAG].n;
+    counts[3] = h->n_qubytes;
+    counts[4] = h->particle_cut;
+    counts[5] = h->n_words;
+    return QMBX_OK;
+}

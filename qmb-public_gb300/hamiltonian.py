@@ -1,0 +1,316 @@
+"""Drop-in replacement for qmb.hamiltonian.Hamiltonian on GB300 GPUs.
+
+Same constructor and methods as qmb/hamiltonian.py:12-206:
+
+* ``Hamiltonian(dict or (site, kind, coef), *, kind="fermi" | "bose2")``
+* ``apply_within(configs_i, psi_i, configs_j)``
+* ``find_relative(configs_i, psi_i, count_selected, configs_exclude=None)``
+* ``diagonal_term(configs)``
+* ``single_relative(configs)``
+
+and the public ``site``, ``kind``, ``coef`` tensors.  Every method runs the
+CUDA kernels of libqmbx.so on the configurations' device through the C ABI
+(include/qmbx.h); tensors on the CPU are rejected (there is no CPU path).
+
+Additions over the reference: complex64 amplitudes select the FP32 path with
+compensated accumulation; ``apply_within`` is differentiable in ``psi_i``
+(its backward is the adjoint kernel); ``apply_within_adjoint`` exposes that
+kernel directly.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from .terms import prepare, sort_terms
+
+__all__ = ["Hamiltonian"]
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _workspace(nbytes: int, device: torch.device) -> torch.Tensor:
+    ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    if ws.data_ptr() % 256:
+        raise RuntimeError("workspace allocation is not 256-byte aligned")
+    return ws
+
+
+class _Table:
+    """A compiled term table: host blob (header read by the host) and its device copy."""
+
+    def __init__(self, site: torch.Tensor, kind: torch.Tensor, coef: torch.Tensor, n_qubytes: int, particle_cut: int,
+                 device: torch.device):
+        lib = _native.library()
+        site = site.detach().to("cpu", torch.int16).contiguous()
+        kind = kind.detach().to("cpu", torch.uint8).contiguous()
+        coef = coef.detach().to("cpu", torch.float64).contiguous()
+        if site.dim() != 2 or site.shape[1] != 4 or kind.shape != site.shape or coef.shape != (site.shape[0], 2):
+            raise RuntimeError("site, kind and coef must have shapes [T, 4], [T, 4] and [T, 2]")
+        nbytes = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_table_bytes(site.data_ptr(), kind.data_ptr(), site.shape[0], n_qubytes, particle_cut,
+                                           ctypes.byref(nbytes)))
+        self.host = torch.empty(nbytes.value, dtype=torch.uint8).pin_memory()
+        _native.check(lib.qmbx_table_build(site.data_ptr(), kind.data_ptr(), coef.data_ptr(), site.shape[0], n_qubytes,
+                                           particle_cut, self.host.data_ptr(), nbytes.value))
+        self.dev = torch.empty(nbytes.value, dtype=torch.uint8, device=device)
+        if self.dev.data_ptr() % 256:
+            raise RuntimeError("table allocation is not 256-byte aligned")
+        self.dev.copy_(self.host, non_blocking=False)
+        counts = (ctypes.c_int64 * 6)()
+        _native.check(lib.qmbx_table_counts(self.host.data_ptr(), counts))
+        self.n_terms, self.n_live, self.n_diag, self.n_qubytes, self.particle_cut, self.n_words = list(counts)
+
+    @property
+    def h(self) -> int:
+        return self.host.data_ptr()
+
+    @property
+    def d(self) -> int:
+        return self.dev.data_ptr()
+
+
+class Hamiltonian:
+    """Second-quantized Hamiltonian over bit-packed configurations (see module docstring)."""
+
+    def __init__(self, hamiltonian: dict | tuple[torch.Tensor, torch.Tensor, torch.Tensor], *, kind: str) -> None:
+        self.site: torch.Tensor
+        self.kind: torch.Tensor
+        self.coef: torch.Tensor
+        if isinstance(hamiltonian, dict):
+            self.site, self.kind, self.coef = sort_terms(*prepare(hamiltonian))
+        else:
+            self.site, self.kind, self.coef = hamiltonian
+        self.particle_cut: int
+        match kind:
+            case "fermi":
+                self.particle_cut = 1
+            case "bose2":
+                self.particle_cut = 2
+            case _:
+                raise ValueError(f"Unknown kind: {kind}")
+        self._tables: dict = {}
+
+    # -- plumbing -----------------------------------------------------------
+
+    def _prepare_data(self, device: torch.device) -> None:
+        """Move the public term tensors to ``device`` as the reference does (qmb/hamiltonian.py:99-102)."""
+        self.site = self.site.to(device=device).contiguous()
+        self.kind = self.kind.to(device=device).contiguous()
+        self.coef = self.coef.to(device=device).contiguous()
+
+    def _table(self, device: torch.device, n_qubytes: int) -> _Table:
+        if device.type != "cuda":
+            raise RuntimeError("this engine runs on CUDA devices only; move the configurations to a GPU")
+        self._prepare_data(device)
+        key = (device.index, n_qubytes, self.site.data_ptr(), self.kind.data_ptr(), self.coef.data_ptr(),
+               self.site._version, self.kind._version, self.coef._version)
+        table = self._tables.get(key)
+        if table is None:
+            with torch.cuda.device(device):
+                table = _Table(self.site, self.kind, self.coef, n_qubytes, self.particle_cut, device)
+            self._tables = {k: v for k, v in self._tables.items() if k[0] != device.index}
+            self._tables[key] = table
+        return table
+
+    @staticmethod
+    def _configs(configs: torch.Tensor, name: str, device: torch.device | None = None) -> torch.Tensor:
+        if configs.dtype != torch.uint8:
+            raise RuntimeError(f"{name} must be uint8.")
+        if configs.dim() != 2:
+            raise RuntimeError(f"{name} must be 2D.")
+        if device is not None and configs.device != device:
+            raise RuntimeError(f"{name} must be on the same device as others.")
+        return configs.contiguous()
+
+    @staticmethod
+    def _amplitudes(psi: torch.Tensor, n: int, name: str, device: torch.device) -> torch.Tensor:
+        if psi.dtype not in (torch.complex128, torch.complex64):
+            raise RuntimeError(f"{name} must be complex128 (or complex64 for the FP32 path).")
+        if psi.dim() != 1 or psi.shape[0] != n:
+            raise RuntimeError(f"{name} must have shape [{n}].")
+        if psi.device != device:
+            raise RuntimeError(f"{name} must be on the same device as others.")
+        return psi.contiguous()
+
+    # -- apply_within ---------------------------------------------------------
+
+    def _apply(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor, *, adjoint: bool,
+               out_dtype: torch.dtype | None = None, include_diagonal: bool = True) -> torch.Tensor:
+        """Forward (psi_i on configs_i -> configs_j) or adjoint (g on configs_j -> configs_i) application."""
+        device = configs_i.device
+        configs_i = self._configs(configs_i, "configs_i")
+        configs_j = self._configs(configs_j, "configs_j", device)
+        nq = configs_i.shape[1]
+        if configs_j.shape[1] != nq:
+            raise RuntimeError("configs_i and configs_j must have the same number of qubytes.")
+        n_i, n_j = configs_i.shape[0], configs_j.shape[0]
+        n_in, n_out = (n_j, n_i) if adjoint else (n_i, n_j)
+        psi = self._amplitudes(psi_i, n_in, "psi", device)
+        table = self._table(device, nq)
+        same = int(configs_i.data_ptr() == configs_j.data_ptr() and n_i == n_j)
+        lib = _native.library()
+        need = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_apply_within_workspace(table.h, n_i, n_j, ctypes.byref(need)))
+        with torch.cuda.device(device):
+            ws = _workspace(need.value, device)
+            stream = _stream(device)
+            if psi.dtype == torch.complex128:
+                out = torch.empty(n_out, dtype=torch.complex128, device=device)
+                name = "qmbx_apply_within_adjoint" if adjoint else "qmbx_apply_within"
+                if adjoint:
+                    args = (table.h, table.d, configs_i.data_ptr(), n_i, configs_j.data_ptr(), psi.data_ptr(), n_j,
+                            same, out.data_ptr(), ws.data_ptr(), ws.numel(), stream)
+                else:
+                    args = (table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j,
+                            same, out.data_ptr(), ws.data_ptr(), ws.numel(), stream)
+                _native.call(name, *args)
+                return out if out_dtype in (None, torch.complex128) else out.to(out_dtype)
+            want64 = out_dtype == torch.complex128
+            out = torch.empty(n_out, dtype=torch.complex128 if want64 else torch.complex64, device=device)
+            o64, o32 = (out.data_ptr(), None) if want64 else (None, out.data_ptr())
+            if adjoint:
+                _native.call("qmbx_apply_within_adjoint_f32c", table.h, table.d, configs_i.data_ptr(), n_i,
+                             configs_j.data_ptr(), psi.data_ptr(), n_j, same, int(include_diagonal), o64, o32,
+                             ws.data_ptr(), ws.numel(), stream)
+            else:
+                _native.call("qmbx_apply_within_f32c", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i,
+                             configs_j.data_ptr(), n_j, same, int(include_diagonal), o64, o32, ws.data_ptr(),
+                             ws.numel(), stream)
+            return out
+
+    def apply_within(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor) -> torch.Tensor:
+        """H psi restricted to configs_j (qmb/hamiltonian.py:104-131); differentiable in psi_i.
+
+        complex128 psi_i gives complex128 (FP64 path); complex64 psi_i gives
+        complex64 computed with compensated FP32 accumulation.
+        """
+        if torch.is_grad_enabled() and psi_i.requires_grad:
+            return _ApplyWithin.apply(self, configs_i, psi_i, configs_j, None)
+        return self._apply(configs_i, psi_i, configs_j, adjoint=False)
+
+    def apply_within_compensated(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor) -> torch.Tensor:
+        """FP32-compensated H psi returned as complex128 (the compensated pair summed exactly); differentiable."""
+        psi_i = psi_i.to(torch.complex64)
+        if torch.is_grad_enabled() and psi_i.requires_grad:
+            return _ApplyWithin.apply(self, configs_i, psi_i, configs_j, torch.complex128)
+        return self._apply(configs_i, psi_i, configs_j, adjoint=False, out_dtype=torch.complex128)
+
+    def apply_within_adjoint(self, configs_i: torch.Tensor, g_j: torch.Tensor, configs_j: torch.Tensor) -> torch.Tensor:
+        """H^dagger applied to g_j on configs_j, restricted to configs_i (the adjoint of apply_within)."""
+        return self._apply(configs_i, g_j, configs_j, adjoint=True)
+
+    # -- find_relative --------------------------------------------------------
+
+    def find_relative(self, configs_i: torch.Tensor, psi_i: torch.Tensor, count_selected: int,
+                      configs_exclude: torch.Tensor | None = None) -> torch.Tensor:
+        """Heaviest connected configurations outside configs_exclude (qmb/hamiltonian.py:133-166)."""
+        if configs_exclude is None:
+            configs_exclude = configs_i
+        device = configs_i.device
+        configs_i = self._configs(configs_i, "configs_i")
+        configs_exclude = self._configs(configs_exclude, "configs_exclude", device)
+        nq = configs_i.shape[1]
+        if configs_exclude.shape[1] != nq:
+            raise RuntimeError("configs_exclude must have the same number of qubytes as configs_i.")
+        psi = self._amplitudes(psi_i, configs_i.shape[0], "psi_i", device).to(torch.complex128)
+        count_selected = int(count_selected)
+        if count_selected < 0:
+            raise RuntimeError("count_selected must not be negative.")
+        table = self._table(device, nq)
+        lib = _native.library()
+        need = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_find_relative_workspace(table.h, configs_i.shape[0], count_selected,
+                                                       configs_exclude.shape[0], ctypes.byref(need)))
+        out = torch.empty((max(count_selected, 1), nq), dtype=torch.uint8, device=device)
+        n_out = ctypes.c_int64(0)
+        with torch.cuda.device(device):
+            stream = _stream(device)
+            for _ in range(4):
+                ws = _workspace(need.value, device)
+                want = ctypes.c_uint64(0)
+                status = lib.qmbx_find_relative(table.h, table.d, configs_i.data_ptr(), psi.data_ptr(),
+                                                configs_i.shape[0], count_selected, configs_exclude.data_ptr(),
+                                                configs_exclude.shape[0], out.data_ptr(), ctypes.byref(n_out),
+                                                ws.data_ptr(), ws.numel(), ctypes.byref(want), stream)
+                if status == _native.QMBX_ERR_WORKSPACE and want.value > need.value:
+                    need = want
+                    del ws
+                    continue
+                _native.check(status)
+                break
+            else:
+                raise RuntimeError("find_relative could not size its workspace")
+        return out[:n_out.value]
+
+    # -- diagonal_term ----------------------------------------------------------
+
+    def diagonal_term(self, configs: torch.Tensor) -> torch.Tensor:
+        """<c|H|c> for every row (qmb/hamiltonian.py:168-186)."""
+        device = configs.device
+        configs = self._configs(configs, "configs")
+        table = self._table(device, configs.shape[1])
+        out = torch.empty(configs.shape[0], dtype=torch.complex128, device=device)
+        with torch.cuda.device(device):
+            _native.call("qmbx_diagonal_term", table.h, table.d, configs.data_ptr(), configs.shape[0], out.data_ptr(),
+                         _stream(device))
+        return out
+
+    # -- single_relative --------------------------------------------------------
+
+    def single_relative(self, configs: torch.Tensor) -> torch.Tensor:
+        """One neighbour per row, drawn with probability proportional to |coef| (qmb/hamiltonian.py:188-206).
+
+        The seed is drawn from torch's CPU generator, as the reference does
+        (qmb/_hamiltonian_cuda.cu:963-964).
+        """
+        device = configs.device
+        configs = self._configs(configs, "configs")
+        table = self._table(device, configs.shape[1])
+        seed = int(torch.randint(0, np.iinfo(np.int64).max, (), dtype=torch.int64))
+        return self.single_relative_seeded(configs, seed)
+
+    def single_relative_seeded(self, configs: torch.Tensor, seed: int) -> torch.Tensor:
+        device = configs.device
+        configs = self._configs(configs, "configs")
+        table = self._table(device, configs.shape[1])
+        lib = _native.library()
+        need = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_single_relative_workspace(table.h, configs.shape[0], ctypes.byref(need)))
+        out = torch.empty_like(configs)
+        with torch.cuda.device(device):
+            ws = _workspace(need.value, device)
+            _native.call("qmbx_single_relative", table.h, table.d, configs.data_ptr(), configs.shape[0],
+                         seed & (2**64 - 1), out.data_ptr(), ws.data_ptr(), ws.numel(), _stream(device))
+        return out
+
+
+class _ApplyWithin(torch.autograd.Function):
+    """y = H psi restricted to configs_j; backward applies H^dagger (the adjoint kernel)."""
+
+    @staticmethod
+    def forward(ctx, ham: Hamiltonian, configs_i, psi_i, configs_j, out_dtype):
+        ctx.ham = ham
+        ctx.in_dtype = psi_i.dtype
+        ctx.save_for_backward(configs_i, configs_j)
+        return ham._apply(configs_i, psi_i.detach(), configs_j, adjoint=False, out_dtype=out_dtype)
+
+    @staticmethod
+    def backward(ctx, grad):
+        configs_i, configs_j = ctx.saved_tensors
+        if grad is None:
+            return None, None, None, None, None
+        g = grad.to(ctx.in_dtype).contiguous()
+        gi = ctx.ham._apply(configs_i, g, configs_j, adjoint=True,
+                            out_dtype=torch.complex128 if ctx.in_dtype == torch.complex128 else None)
+        return None, None, gi.to(ctx.in_dtype), None, None

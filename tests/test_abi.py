@@ -1,0 +1,187 @@
+"""The C ABI library: it loads without a GPU, exports every declared symbol, and
+its host-side term compiler reproduces the reference's operator walk."""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import REPO, golden
+
+native = __import__("qmb_gb300._native", fromlist=["library"])
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import importlib
+
+    importlib.import_module("qmb-public_gb300._build").build()
+    return native.library()
+
+
+def declared_symbols() -> list[str]:
+    text = open(os.path.join(REPO, "include", "qmbx.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(qmbx_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(native.SIGNATURES), "the ctypes binding must cover exactly the header"
+
+
+def test_version_and_no_error(lib):
+    assert lib.qmbx_version() >= 10000
+    assert lib.qmbx_last_error() == b""
+
+
+class Part(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("off_test", ctypes.c_uint64), ("off_apply", ctypes.c_uint64),
+                ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
+                ("off_norm", ctypes.c_uint64)]
+
+
+class Header(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_uint32), ("version", ctypes.c_uint32), ("n_qubytes", ctypes.c_int32),
+                ("particle_cut", ctypes.c_int32), ("n_words", ctypes.c_int32), ("n_sites", ctypes.c_int32),
+                ("n_terms", ctypes.c_int64), ("n_live", ctypes.c_int64), ("part", Part * 3),
+                ("total_bytes", ctypes.c_uint64)]
+
+
+def compile_table(lib, site, kind, coef, nq, pc):
+    site = np.ascontiguousarray(site, dtype=np.int16)
+    kind = np.ascontiguousarray(kind, dtype=np.uint8)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nbytes = ctypes.c_uint64()
+    native.check(lib.qmbx_table_bytes(site.ctypes.data, kind.ctypes.data, site.shape[0], nq, pc, ctypes.byref(nbytes)))
+    blob = np.zeros(nbytes.value, dtype=np.uint8)
+    native.check(lib.qmbx_table_build(site.ctypes.data, kind.ctypes.data, coef.ctypes.data, site.shape[0], nq, pc,
+                                      blob.ctypes.data, blob.size))
+    return blob
+
+
+def read_part(blob, h, which):
+    p = h.part[which]
+    w = h.n_words
+    n = p.n
+
+    def arr(off, dtype, count):
+        return np.frombuffer(blob, dtype=dtype, count=count, offset=off)
+
+    test = arr(p.off_test, np.uint64, n * 2 * w).reshape(n, w, 2)
+    apply = arr(p.off_apply, np.uint64, n * 2 * w).reshape(n, w, 2)
+    coef = arr(p.off_coef, np.float64, n * 2).reshape(n, 2)
+    orig = arr(p.off_orig, np.int32, n)
+    return test, apply, coef, orig
+
+
+def to_key(row: np.ndarray, w: int) -> list[int]:
+    padded = np.zeros(8 * w, dtype=np.uint8)
+    padded[:row.size] = row
+    return [int.from_bytes(bytes(padded[8 * q:8 * q + 8]), "big") for q in range(w)]
+
+
+def from_key(key: list[int], nq: int) -> np.ndarray:
+    raw = b"".join(k.to_bytes(8, "big") for k in key)
+    return np.frombuffer(raw[:nq], dtype=np.uint8).copy()
+
+
+def closed_form(test, apply, key):
+    for q, word in enumerate(key):
+        mask, val = int(test[q, 0]), int(test[q, 1])
+        if (word ^ val) & mask:
+            return None
+    image = [word ^ int(apply[q, 0]) for q, word in enumerate(key)]
+    parity = sum(bin(word & int(apply[q, 1])).count("1") for q, word in enumerate(key)) & 1
+    return image, parity
+
+
+@pytest.mark.parametrize("case", ["random_terms_fermi", "random_terms_bose2", "ab_initio_6", "ising_4x4", "hubbard_3x2"])
+def test_compiled_terms_reproduce_the_operator_walk(lib, case):
+    g = golden(case)
+    site, kind, coef = g["site"], g["kind"], g["coef"]
+    pc = int(g["particle_cut"])
+    rows = np.concatenate([g["configs_i"], g["configs_j"]])[:120]
+    nq = rows.shape[1]
+    blob = compile_table(lib, site, kind, coef, nq, pc)
+    h = Header.from_buffer_copy(blob[:ctypes.sizeof(Header)].tobytes())
+    assert h.n_words == (nq + 7) // 8
+    fwd = read_part(blob, h, 0)
+    adj = read_part(blob, h, 1)
+    diag = read_part(blob, h, 2)
+    assert fwd[0].shape[0] == adj[0].shape[0]
+    # every live term appears exactly once, in input order within each part
+    live = []
+    for part in (fwd, diag):
+        live.extend(part[3].tolist())
+        assert list(part[3]) == sorted(part[3])
+    for t in range(site.shape[0]):
+        ok_any = any(oracle.apply_term(site[t], kind[t], r, pc)[0] for r in rows[:40])
+        if ok_any:
+            assert t in live
+    for part_name, (test, apply, cf, orig) in (("fwd", fwd), ("diag", diag)):
+        for slot in range(len(orig)):
+            t = int(orig[slot])
+            for r in rows:
+                ok, parity, out = oracle.apply_term(site[t], kind[t], r, pc)
+                got = closed_form(test[slot], apply[slot], to_key(r, h.n_words))
+                assert (got is not None) == ok, (part_name, t)
+                if not ok:
+                    continue
+                image, par = got
+                assert np.array_equal(from_key(image, nq), out)
+                # the stored coefficient carries the constant part of the sign
+                sign = -1.0 if parity else 1.0
+                stored_sign = -1.0 if par else 1.0
+                np.testing.assert_array_equal(cf[slot] * stored_sign, coef[t] * sign)
+                if part_name == "diag":
+                    assert np.array_equal(out, r)
+    # the adjoint part maps every image back to its source with the same sign
+    test_a, apply_a, cf_a, orig_a = adj
+    for slot in range(len(orig_a)):
+        t = int(orig_a[slot])
+        for r in rows[:60]:
+            ok, parity, out = oracle.apply_term(site[t], kind[t], r, pc)
+            if not ok:
+                continue
+            back = closed_form(test_a[slot], apply_a[slot], to_key(out, h.n_words))
+            assert back is not None
+            image, par = back
+            assert np.array_equal(from_key(image, nq), r)
+            assert np.array_equal(cf_a[slot] * (-1.0 if par else 1.0), coef[t] * (-1.0 if parity else 1.0))
+
+
+def test_table_rejects_bad_input(lib):
+    site = np.array([[0, 1, 0, 0]], dtype=np.int16)
+    kind = np.array([[1, 0, 2, 2]], dtype=np.uint8)
+    nbytes = ctypes.c_uint64()
+    assert lib.qmbx_table_bytes(site.ctypes.data, kind.ctypes.data, 1, 0, 1, ctypes.byref(nbytes)) == native.QMBX_ERR_ARGUMENT
+    assert b"n_qubytes" in lib.qmbx_last_error()
+    assert lib.qmbx_table_bytes(site.ctypes.data, kind.ctypes.data, 1, 1, 3, ctypes.byref(nbytes)) == native.QMBX_ERR_ARGUMENT
+    bad_site = np.array([[8, 1, 0, 0]], dtype=np.int16)
+    assert lib.qmbx_table_bytes(bad_site.ctypes.data, kind.ctypes.data, 1, 1, 1, ctypes.byref(nbytes)) == native.QMBX_ERR_ARGUMENT
+    assert b"site 8" in lib.qmbx_last_error()
+    bad_kind = np.array([[0, 1, 0, 0]], dtype=np.uint8) + 3
+    assert lib.qmbx_table_bytes(site.ctypes.data, bad_kind.ctypes.data, 1, 1, 1, ctypes.byref(nbytes)) == native.QMBX_ERR_ARGUMENT
+    # empty slots may hold any site value (the reference leaves them uninitialised)
+    garbage = np.array([[3, 1, -77, 900]], dtype=np.int16)
+    assert lib.qmbx_table_bytes(garbage.ctypes.data, kind.ctypes.data, 1, 1, 1, ctypes.byref(nbytes)) == native.QMBX_OK
+    assert lib.qmbx_last_error() == b""
+
+
+def test_dead_terms_are_dropped(lib):
+    # a+_1 a+_1 can never apply; a+_2 a_2 is diagonal; a+_3 a_1 changes the row
+    site = np.array([[1, 1, 0, 0], [2, 2, 0, 0], [3, 1, 0, 0]], dtype=np.int16)
+    kind = np.array([[1, 1, 2, 2], [1, 0, 2, 2], [1, 0, 2, 2]], dtype=np.uint8)
+    coef = np.ones((3, 2))
+    blob = compile_table(lib, site, kind, coef, 1, 1)
+    counts = (ctypes.c_int64 * 6)()
+    native.check(lib.qmbx_table_counts(blob.ctypes.data, counts))
+    assert list(counts) == [3, 2, 1, 1, 1, 1]
