@@ -1,0 +1,420 @@
+"""Benchmark of the Hamiltonian engine's hot path on one GB300.
+
+Default workload (``--workload c2``): a synthetic ab-initio Hamiltonian on 28
+spin orbitals (14 spatial, n_qubytes 4; 55,371 normal-ordered terms from
+seeded integrals), configs_i = 20,000 and configs_j = 200,000 unique random
+determinants with 5 alpha + 5 beta electrons, complex N(0,1) amplitudes.
+
+One step is the FP32-compensated apply_within forward (configs_i ->
+configs_j) followed by its adjoint (configs_j -> configs_i), i.e. the work of
+one energy-gradient evaluation.  The metric is term applications per second,
+T * (N_i + N_j) per step (the reference's thread grid is T * N_i for a
+forward application).  The same line reports the FP64 path, find_relative
+(top 50,000 excluding configs_i), the energy error of the FP32 path, the
+end-to-end rate through the public API with host buffers, the roofline of the
+enumeration kernel, and the CPU oracle's rate on the host cores.
+
+``--impl reference`` times the CPU restatement of the reference engine
+(oracle/, the reference's own CPU code cannot be built on the GPU host) on a
+bounded sample of the same workload with every host core.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import multiprocessing as mp
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    "c2": dict(n_orbit=14, n_alpha=5, n_beta=5, n_i=20000, n_j=200000, count_selected=50000, seed=2024,
+               description="ab-initio 28 spin orbitals (n_qubytes 4), 5a+5b, N_i 20000, N_j 200000, K 50000"),
+    "c1": dict(n_orbit=6, n_alpha=3, n_beta=3, n_i=400, n_j=400, count_selected=100, seed=2024,
+               description="ab-initio 12 spin orbitals (n_qubytes 2), 3a+3b, all 400 determinants"),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+
+def make_workload(name: str):
+    import numpy as np
+
+    qmb = importlib.import_module("qmb-public_gb300")
+    terms = qmb.terms
+    w = WORKLOADS[name]
+    site, kind, coef = terms.integral_hamiltonian_tables(w["n_orbit"], seed=w["seed"])
+    if w["n_i"] == w["n_j"] and name == "c1":
+        ci = terms.all_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"])
+        cj = ci
+    else:
+        ci = terms.random_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"], w["n_i"], seed=w["seed"] + 1)
+        cj = terms.random_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"], w["n_j"], seed=w["seed"] + 2)
+    psi = terms.random_psi(ci.shape[0], seed=w["seed"] + 3)
+    return dict(site=site.numpy(), kind=kind.numpy(), coef=coef.numpy(), configs_i=ci, configs_j=cj, psi=psi,
+                n_terms=int(site.shape[0]), nq=int(ci.shape[1]), spec=w)
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle timing (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+
+
+def _oracle_worker(args):
+    site, kind, coef, rows, psi, configs_j, budget_s, chunk = args
+    sys.path.insert(0, REPO)
+    import oracle
+
+    done = 0
+    start = time.perf_counter()
+    while done < rows.shape[0] and time.perf_counter() - start < budget_s:
+        hi = min(done + chunk, rows.shape[0])
+        oracle.apply_within(site, kind, coef, rows[done:hi], psi[done:hi], configs_j)
+        done = hi
+    return done, time.perf_counter() - start
+
+
+def oracle_rate(wl, budget_s: float, cores: int | None = None) -> dict:
+    """Term applications per second of the CPU oracle's apply_within, every host core on a row slice."""
+    import numpy as np
+
+    import oracle
+
+    oracle.build()
+    cores = cores or os.cpu_count() or 1
+    rows = wl["configs_i"]
+    psi = wl["psi"]
+    slices = np.array_split(np.arange(rows.shape[0]), cores)
+    chunk = 16
+    jobs = [(wl["site"], wl["kind"], wl["coef"], rows[s], psi[s], wl["configs_j"], budget_s, chunk) for s in slices]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        results = pool.map(_oracle_worker, jobs)
+    done = sum(r[0] for r in results)
+    elapsed = max(r[1] for r in results)
+    rate = wl["n_terms"] * done / elapsed
+    return {"value": rate, "unit": "term-applications/s", "cores": cores, "kind": "port",
+            "sample": f"apply_within forward of {done} of {rows.shape[0]} configs_i rows against all "
+                      f"{wl['configs_j'].shape[0]} configs_j, {cores} processes, {elapsed:.1f} s"}
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per enumeration launch from the committed ncu summary, or None."""
+    path = os.path.join(REPO, "profiles", f"enumerate_kernel_{workload}.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def run_ours(args, wl, rank: int, world: int) -> dict | None:
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    qmb = importlib.import_module("qmb-public_gb300")
+    native = importlib.import_module("qmb-public_gb300._native")
+    device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(device)
+    ham = qmb.Hamiltonian((torch.from_numpy(wl["site"]), torch.from_numpy(wl["kind"]), torch.from_numpy(wl["coef"])),
+                          kind="fermi")
+    ci = torch.from_numpy(wl["configs_i"]).to(device)
+    cj = torch.from_numpy(wl["configs_j"]).to(device)
+    psi64 = torch.from_numpy(wl["psi"]).to(device)
+    psi32 = psi64.to(torch.complex64)
+    n_i, n_j, T, nq = ci.shape[0], cj.shape[0], wl["n_terms"], wl["nq"]
+    units = T * (n_i + n_j)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)  # > 129 MB of L2
+    stream = torch.cuda.current_stream(device)
+
+    def step32():
+        y = ham.apply_within_compensated(ci, psi32, cj)
+        return ham.apply_within_adjoint(ci, y.to(torch.complex64), cj)
+
+    def step64():
+        y = ham.apply_within(ci, psi64, cj)
+        return ham.apply_within_adjoint(ci, y, cj)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(fn, steps):
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            times.append((a, b))
+        torch.cuda.synchronize(device)
+        return sum(a.elapsed_time(b) for a, b in times)
+
+    for _ in range(args.warmup):
+        step32()
+        step64()
+    torch.cuda.synchronize(device)
+
+    # headline: FP32-compensated forward + adjoint, profiled per kernel group
+    native.profile_enable(True)
+    launches0 = native.profile_read()["launches"]
+    barrier()
+    torch.cuda.synchronize(device)
+    with ClockSampler(device.index) as clocks:
+        ms32 = timed(step32, args.steps)
+    barrier()
+    torch.cuda.synchronize(device)
+    prof = native.profile_read()
+    native.profile_enable(False)
+    launches = prof["launches"] - launches0
+    n_enum, ms_enum = prof["groups"]["enumerate"]
+
+    ms64 = timed(step64, args.steps)
+
+    if world > 1:
+        t = torch.tensor([ms32, ms64], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32, ms64 = float(t[0]), float(t[1])
+
+    # find_relative (top K excluding configs_i)
+    K = wl["spec"]["count_selected"]
+    ham.find_relative(ci, psi64, K)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    reps = max(1, min(args.steps, 5))
+    for _ in range(reps):
+        rel = ham.find_relative(ci, psi64, K)
+    torch.cuda.synchronize(device)
+    ms_rel = (time.perf_counter() - t0) * 1e3 / reps
+
+    # energy error of the FP32 path on the configs_i block
+    e64 = float(qmb.variational_energy(ham, ci, psi32.to(torch.complex128)))
+    e32 = float(qmb.variational_energy(ham, ci, psi32))
+
+    # end to end through the public API with host buffers
+    ci_h = torch.from_numpy(wl["configs_i"]).pin_memory()
+    cj_h = torch.from_numpy(wl["configs_j"]).pin_memory()
+    psi_h = torch.from_numpy(wl["psi"]).to(torch.complex64).pin_memory()
+    y_h = torch.empty(n_j, dtype=torch.complex128).pin_memory()
+    x_h = torch.empty(n_i, dtype=torch.complex64).pin_memory()
+
+    def step_e2e():
+        a_i = ci_h.to(device, non_blocking=True)
+        a_j = cj_h.to(device, non_blocking=True)
+        p = psi_h.to(device, non_blocking=True)
+        y = ham.apply_within_compensated(a_i, p, a_j)
+        x = ham.apply_within_adjoint(a_i, y.to(torch.complex64), a_j)
+        y_h.copy_(y, non_blocking=True)
+        x_h.copy_(x, non_blocking=True)
+
+    step_e2e()
+    ms_e2e = timed(step_e2e, args.steps)
+    h2d = ci_h.numel() + cj_h.numel() + psi_h.numel() * 8
+    d2h = y_h.numel() * 16 + x_h.numel() * 8
+
+    if rank != 0:
+        return None
+    cpu = oracle_rate(wl, budget_s=args.cpu_seconds) if world == 1 else None
+
+    # roofline of the enumeration kernel: algorithmic bytes per launch
+    # forward: targets N_j (key + FP64 result), sources N_i (key + FP32 amplitude), terms T (28 B)
+    # adjoint: the same with the two sets swapped
+    alg_fwd = n_j * (nq + 16) + n_i * (nq + 8) + T * 28
+    alg_adj = n_i * (nq + 16) + n_j * (nq + 8) + T * 28
+    alg = (alg_fwd + alg_adj) / 2
+    per_launch_ms = ms_enum / max(n_enum, 1)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    ms_step32 = ms32 / args.steps
+    value = world * units / (ms_step32 * 1e-3)
+    line = {
+        "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
+        "value": value,
+        "unit": "term-applications/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step32,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": T, "n_i": n_i, "n_j": n_j,
+                   "n_qubytes": nq, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MB write) before every timed step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": ncu_traffic(args.workload), "kernel": "enumerate_kernel",
+                     "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_ms,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * units / (ms_e2e / args.steps * 1e-3), "unit": "term-applications/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "fp64": {"value": world * units / (ms64 / args.steps * 1e-3), "ms_per_step": ms64 / args.steps},
+        "speedup_fp32c_vs_fp64": ms64 / ms32,
+        "find_relative": {"ms": ms_rel, "count_selected": K, "rows_out": int(rel.shape[0])},
+        "energy": {"fp64": e64, "fp32c": e32, "abs_error_ha": abs(e32 - e64)},
+        "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]},
+    }
+    return line
+
+
+def run_reference(args, wl) -> dict:
+    cpu = oracle_rate(wl, budget_s=args.cpu_seconds)
+    value = cpu["value"]
+    return {
+        "impl": "reference",
+        "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
+        "value": value,
+        "unit": "term-applications/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wl["n_terms"] * (wl["configs_i"].shape[0] + wl["configs_j"].shape[0]) / value * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": wl["n_terms"],
+                   "n_i": int(wl["configs_i"].shape[0]), "n_j": int(wl["configs_j"].shape[0]),
+                   "n_qubytes": wl["nq"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "term-applications/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    parser = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=10)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    parser.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    parser.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU oracle sample")
+    args = parser.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        wl = make_workload(args.workload)
+        print(json.dumps(run_reference(args, wl)), flush=True)
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    wl = make_workload(args.workload)
+    line = run_ours(args, wl, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

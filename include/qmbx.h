@@ -165,6 +165,21 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
                          uint64_t seed, uint8_t* out, void* workspace, uint64_t workspace_bytes,
                          qmbx_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Tracing (no counterpart in the reference, which has none).
+ * Every kernel launch of this library increments a process-wide counter.
+ * qmbx_profile_enable(1) additionally brackets the launches of four groups
+ * (0 term enumeration, 1 key packing/sorting, 2 selection, 3 other) with
+ * CUDA events on the launching stream and resets the totals;
+ * qmbx_profile_read waits for the recorded events and returns the launch
+ * counter and, per group, the number of timed launches and their total
+ * milliseconds (arrays of 4).
+ * ------------------------------------------------------------------------- */
+
+int qmbx_profile_enable(int32_t on);
+
+int qmbx_profile_read(int64_t* launches, int64_t* counts, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,7 +45,26 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_find_relative": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _I64, _P, _PI64, _P, _U64, _PU64, _P]),
     "qmbx_single_relative_workspace": (ctypes.c_int, [_P, _I64, _PU64]),
     "qmbx_single_relative": (ctypes.c_int, [_P, _P, _P, _I64, _U64, _P, _P, _U64, _P]),
+    "qmbx_profile_enable": (ctypes.c_int, [_I32]),
+    "qmbx_profile_read": (ctypes.c_int, [_PI64, _PI64, ctypes.POINTER(ctypes.c_double)]),
 }
+
+PROFILE_GROUPS = ("enumerate", "keys", "select", "other")
+
+
+def profile_enable(on: bool) -> None:
+    """Start (and reset) or stop per-group kernel timing with CUDA events."""
+    check(library().qmbx_profile_enable(1 if on else 0))
+
+
+def profile_read() -> dict:
+    """Launch counter and per-group (count, milliseconds) since the last profile_enable."""
+    launches = ctypes.c_int64()
+    counts = (ctypes.c_int64 * 4)()
+    ms = (ctypes.c_double * 4)()
+    check(library().qmbx_profile_read(ctypes.byref(launches), counts, ms))
+    return {"launches": launches.value,
+            "groups": {g: (counts[k], ms[k]) for k, g in enumerate(PROFILE_GROUPS)}}
 
 
 class QmbxError(RuntimeError):

@@ -313,18 +313,18 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     if (a.prec == Prec::F64) {
         const double2* in = static_cast<const double2*>(a.in);
         if (a.adjoint) {
-            first_value_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (double2*)uval);
+            QMBX_KERNEL(kGroupOther, s, first_value_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (double2*)uval));
         } else {
-            run_sum_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
-                                                                  (double2*)uval);
+            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
+                                                                  (double2*)uval));
         }
     } else {
         const float2* in = static_cast<const float2*>(a.in);
         if (a.adjoint) {
-            first_value_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (float2*)uval);
+            QMBX_KERNEL(kGroupOther, s, first_value_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (float2*)uval));
         } else {
-            run_sum_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
-                                                                 (float2*)uval);
+            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
+                                                                 (float2*)uval));
         }
     }
     QMBX_LAUNCH_CHECK("amplitude gather");
@@ -338,22 +338,22 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         if (!a.adjoint) {
             GatherF64<W, false> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
                                   walk.first, nullptr, nullptr};
-            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         } else {
             GatherF64<W, true> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
                                  nullptr, walk.start, walk.perm};
-            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         }
     } else {
         if (!a.include_diag) diag.n = 0;
         if (!a.adjoint) {
             GatherF32C<W, false> v{look.keys,  look.count, (const float2*)uval, walk_part.coef32, diag.coef,
                                    a.include_diag, a.out64, a.out32, walk.first, nullptr, nullptr};
-            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         } else {
             GatherF32C<W, true> v{look.keys, look.count, (const float2*)uval, walk_part.coef32, diag.coef,
                                   a.include_diag, a.out64, a.out32, nullptr, walk.start, walk.perm};
-            enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag);
+            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         }
     }
     QMBX_LAUNCH_CHECK("apply_within enumeration");
@@ -413,7 +413,7 @@ int diagonal_impl(const void* table_host, const void* table_dev, const uint8_t* 
     PartView diag = part_view(table_host, table_dev, QMBX_PART_DIAG);
     DiagonalF64<W> v{diag.coef, out};
     ByteRows<W> src{configs, h->n_qubytes};
-    enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag);
+    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));
     QMBX_LAUNCH_CHECK("diagonal_term enumeration");
     return QMBX_OK;
 }

@@ -7,6 +7,7 @@
 #include "../../include/qmbx.h"
 #include "common.h"
 #include "format.h"
+#include "profile.h"
 
 #define QMBX_CUDA_TRY(expr)                                                                          \
     do {                                                                                             \

@@ -49,7 +49,7 @@ __global__ void unpack_kernel(const uint64_t* __restrict__ keys, const int* __re
 template <int W>
 int pack_rows(const uint8_t* rows, int64_t n, int nq, uint64_t* keys, cudaStream_t s) {
     if (n == 0) return QMBX_OK;
-    pack_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(rows, n, nq, keys);
+    QMBX_KERNEL(kGroupKeys, s, pack_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(rows, n, nq, keys));
     QMBX_LAUNCH_CHECK("pack_kernel");
     return QMBX_OK;
 }
@@ -57,7 +57,7 @@ int pack_rows(const uint8_t* rows, int64_t n, int nq, uint64_t* keys, cudaStream
 template <int W>
 int unpack_rows(const uint64_t* keys, const int* n_rows, int64_t n_max, int nq, uint8_t* rows, cudaStream_t s) {
     if (n_max == 0) return QMBX_OK;
-    unpack_kernel<W><<<grid_for(n_max, kThreads), kThreads, 0, s>>>(keys, n_rows, n_max, nq, rows);
+    QMBX_KERNEL(kGroupKeys, s, unpack_kernel<W><<<grid_for(n_max, kThreads), kThreads, 0, s>>>(keys, n_rows, n_max, nq, rows));
     QMBX_LAUNCH_CHECK("unpack_kernel");
     return QMBX_OK;
 }
@@ -165,10 +165,10 @@ int64_t scan_scratch(int64_t n) {
 
 int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s) {
     int64_t nb = scan_scratch(n);
-    if (n > 0) scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch);
-    else set_zero_kernel<<<1, 1, 0, s>>>(scratch);
-    scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total);
-    if (n > 0) scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, scratch);
+    if (n > 0) QMBX_KERNEL(kGroupKeys, s, scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch));
+    else QMBX_KERNEL(kGroupKeys, s, set_zero_kernel<<<1, 1, 0, s>>>(scratch));
+    QMBX_KERNEL(kGroupKeys, s, scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total));
+    if (n > 0) QMBX_KERNEL(kGroupKeys, s, scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, scratch));
     QMBX_LAUNCH_CHECK("exclusive_scan");
     return QMBX_OK;
 }
@@ -293,7 +293,7 @@ int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_o
     const int nblocks = sort_blocks<W>(n);
     if (n_bytes == 0) {
         QMBX_CUDA_TRY(cudaMemcpyAsync(keys_out, keys_in, n * W * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
-        identity_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(vals_in, vals_out, n);
+        QMBX_KERNEL(kGroupKeys, s, identity_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(vals_in, vals_out, n));
         QMBX_LAUNCH_CHECK("identity_kernel");
         return QMBX_OK;
     }
@@ -306,11 +306,11 @@ int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_o
         bool to_out = ((n_bytes - 1 - p) & 1) == 0;
         uint64_t* dst_k = to_out ? keys_out : sc.keys;
         int32_t* dst_v = to_out ? vals_out : sc.vals;
-        radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks);
+        QMBX_KERNEL(kGroupKeys, s, radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
         int st = exclusive_scan(sc.counts, sc.counts, (int64_t)256 * nblocks, nullptr, sc.scan, s);
         if (st != QMBX_OK) return st;
-        radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
-                                                                 nblocks);
+        QMBX_KERNEL(kGroupKeys, s, radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
+                                                                 nblocks));
         QMBX_LAUNCH_CHECK("radix sort pass");
         src_k = dst_k;
         src_v = dst_v;
@@ -379,17 +379,17 @@ template <int W>
 int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     const int64_t n = out.n;
     if (n == 0) {
-        set_int_kernel<<<1, 1, 0, s>>>(out.count, 0);
+        QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
         QMBX_LAUNCH_CHECK("set_int_kernel");
         return QMBX_OK;
     }
     int st;
     if ((st = pack_rows<W>(rows, n, nq, out.packed, s)) != QMBX_OK) return st;
     if ((st = sort_pairs<W>(out.packed, nullptr, out.sorted_keys, out.perm, n, nq, out.sort, s)) != QMBX_OK) return st;
-    head_flags_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, n, out.head);
+    QMBX_KERNEL(kGroupKeys, s, head_flags_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, n, out.head));
     if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.sort.scan, s)) != QMBX_OK) return st;
-    compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
-                                                                       out.keys, out.first, out.start, out.count);
+    QMBX_KERNEL(kGroupKeys, s, compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
+                                                                       out.keys, out.first, out.start, out.count));
     QMBX_LAUNCH_CHECK("build_rowset");
     return QMBX_OK;
 }

@@ -1,0 +1,37 @@
+// Launch counting and per-group kernel timing (see profile.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace qmbx {
+
+enum ProfileGroup { kGroupEnumerate = 0, kGroupKeys = 1, kGroupSelect = 2, kGroupOther = 3, kProfileGroups = 4 };
+
+void note_launch(int n);
+
+// Brackets the launches made during its lifetime with events on `stream`
+// when profiling is enabled; does nothing otherwise.
+class Timing {
+   public:
+    Timing(int group, cudaStream_t stream);
+    ~Timing();
+    Timing(const Timing&) = delete;
+    Timing& operator=(const Timing&) = delete;
+
+   private:
+    int group_;
+    cudaStream_t stream_;
+    cudaEvent_t start_ = nullptr;
+    cudaEvent_t stop_ = nullptr;
+};
+
+}  // namespace qmbx
+
+// Launch one kernel (the variadic argument is the launch expression) inside a
+// timing scope of the given group and count it.
+#define QMBX_KERNEL(group, stream, ...)               \
+    do {                                              \
+        ::qmbx::Timing qmbx_timing_((group), (stream)); \
+        __VA_ARGS__;                                  \
+        ::qmbx::note_launch(1);                       \
+    } while (0)

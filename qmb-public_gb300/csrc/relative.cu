@@ -245,7 +245,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     int st;
     if ((st = build_rowset<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
     if ((st = pack_rows<W>(a.configs_i, a.n_i, nq, L.keys_i, s)) != QMBX_OK) return st;
-    zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1);
+    QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
     QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
 
     RelativeArgs r{};
@@ -258,7 +258,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
     const unsigned grid = grid_for(a.n_i, kThreads);
-    relative_kernel<W, false><<<grid, kThreads, 0, s>>>(r);
+    QMBX_KERNEL(kGroupEnumerate, s, relative_kernel<W, false><<<grid, kThreads, 0, s>>>(r));
     QMBX_LAUNCH_CHECK("find_relative histogram pass");
 
     std::vector<unsigned long long> hist(kBuckets);
@@ -292,7 +292,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.emit_rank = L.emit_rank;
     r.emit_keys = L.emit_keys;
     r.overflow = L.overflow;
-    relative_kernel<W, true><<<grid, kThreads, 0, s>>>(r);
+    QMBX_KERNEL(kGroupEnumerate, s, relative_kernel<W, true><<<grid, kThreads, 0, s>>>(r));
     QMBX_LAUNCH_CHECK("find_relative emission pass");
     unsigned long long n_emit = 0;
     int overflow = 0;
@@ -308,8 +308,8 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         return st;
     }
     const int64_t keep = e < k ? e : k;
-    gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
-                                                                            L.sel_keys);
+    QMBX_KERNEL(kGroupSelect, s, gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
+                                                                            L.sel_keys));
     QMBX_LAUNCH_CHECK("gather_selected_kernel");
     // sort and de-duplicate the selected rows: unpack to bytes in the output
     // buffer, then build a row set from those bytes
@@ -412,14 +412,14 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     int st;
     if ((st = build_rowset<W>(configs, h->n_qubytes, L.set, s)) != QMBX_OK) return st;
     if (off.n > 0) {
-        es_factor_kernel<<<grid_for(off.n, kThreads), kThreads, 0, s>>>(off.coef, off.orig, off.n, seed, L.kf);
+        QMBX_KERNEL(kGroupOther, s, es_factor_kernel<<<grid_for(off.n, kThreads), kThreads, 0, s>>>(off.coef, off.orig, off.n, seed, L.kf));
         QMBX_LAUNCH_CHECK("es_factor_kernel");
     }
     PartView none = off;
     none.n = 0;
     SingleVisitor<W> v{L.set.keys, L.set.count, L.kf, off.orig, out, h->n_qubytes};
     KeyRows<W> src{L.set.packed};
-    enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none);
+    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
     QMBX_LAUNCH_CHECK("single_relative enumeration");
     return QMBX_OK;
 }

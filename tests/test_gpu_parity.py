@@ -21,9 +21,10 @@ RTOL_F64 = 1e-12
 
 
 def abs_scale(site, kind, coef, configs_i, psi_i, configs_j, pc):
+    """Per-target sum of |coef*psi| over contributing pairs (particle_cut 2 drops the signs)."""
     mag = np.zeros_like(coef)
     mag[:, 0] = np.hypot(coef[:, 0], coef[:, 1])
-    return np.abs(oracle.apply_within(site, kind, mag, configs_i, np.abs(psi_i).astype(np.complex128), configs_j, pc))
+    return np.abs(oracle.apply_within(site, kind, mag, configs_i, np.abs(psi_i).astype(np.complex128), configs_j, 2))
 
 
 def ham_of(g):

@@ -17,11 +17,14 @@ from conftest import GOLDEN_CASES, golden
 
 
 def abs_sum_bound(site, kind, coef, configs_i, psi_i, configs_j, particle_cut):
-    """Per-target sum of |coef*psi| over contributing pairs (the tolerance scale)."""
+    """Per-target sum of |coef*psi| over contributing pairs (the tolerance scale).
+
+    particle_cut 2 applies the same operators without the fermionic sign, so
+    nothing cancels.
+    """
     mag_coef = np.zeros_like(coef)
     mag_coef[:, 0] = np.hypot(coef[:, 0], coef[:, 1])
-    return np.abs(oracle.apply_within(site, kind, mag_coef, configs_i, np.abs(psi_i).astype(np.complex128), configs_j,
-                                      particle_cut))
+    return np.abs(oracle.apply_within(site, kind, mag_coef, configs_i, np.abs(psi_i).astype(np.complex128), configs_j, 2))
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
