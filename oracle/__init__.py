@@ -73,7 +73,8 @@ def _table(site, kind, coef):
 
 
 def _psi(psi) -> np.ndarray:
-    return _c(np.asarray(psi, dtype=np.complex128).view(np.float64).reshape(-1, 2), np.float64)
+    flat = np.ascontiguousarray(np.asarray(psi, dtype=np.complex128).reshape(-1))
+    return _c(flat.view(np.float64).reshape(-1, 2), np.float64)
 
 
 def apply_term(site_row, kind_row, config, particle_cut: int = 1):

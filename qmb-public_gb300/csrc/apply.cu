@@ -94,8 +94,7 @@ __device__ __forceinline__ void comp_cmul_add(CompSum& re, CompSum& im, float4 c
 // Values of the looked-up rows sit in val[u] for unique key u of lookup.
 template <int W, bool CONJ>
 struct GatherF64 {
-    const uint64_t* lookup;  // sorted unique keys of the looked-up row set
-    const int* n_lookup;
+    HashView lookup;         // hash set over the unique keys of the looked-up row set
     const double2* val;      // one amplitude per unique looked-up key
     const double2* coef;     // coefficients of the walked part
     const double2* dcoef;    // coefficients of the diagonal part
@@ -105,14 +104,10 @@ struct GatherF64 {
     const int32_t* run_perm;
     struct Acc {
         double re, im, dre, dim;
-        int64_t n;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
-        a.re = a.im = a.dre = a.dim = 0.0;
-        a.n = *n_lookup;
-    }
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const { a.re = a.im = a.dre = a.dim = 0.0; }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        int64_t pos = find_key<W>(lookup, a.n, img);
+        int64_t pos = hash_find<W>(lookup, img);
         if (pos < 0) return;
         double2 cf = __ldg(coef + slot);
         double2 p = __ldg(val + pos);
@@ -134,7 +129,7 @@ struct GatherF64 {
     }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         if (a.dre != 0.0 || a.dim != 0.0) {
-            int64_t pos = find_key<W>(lookup, a.n, c);
+            int64_t pos = hash_find<W>(lookup, c);
             if (pos >= 0) {
                 double2 p = __ldg(val + pos);
                 a.re += a.dre * p.x - a.dim * p.y;
@@ -152,8 +147,7 @@ struct GatherF64 {
 
 template <int W, bool CONJ>
 struct GatherF32C {
-    const uint64_t* lookup;
-    const int* n_lookup;
+    HashView lookup;
     const float2* val;
     const float4* coef32;
     const double2* dcoef;
@@ -166,16 +160,14 @@ struct GatherF32C {
     struct Acc {
         CompSum re, im;
         double dre, dim;
-        int64_t n;
     };
     __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
         a.re.zero();
         a.im.zero();
         a.dre = a.dim = 0.0;
-        a.n = *n_lookup;
     }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        int64_t pos = find_key<W>(lookup, a.n, img);
+        int64_t pos = hash_find<W>(lookup, img);
         if (pos < 0) return;
         comp_cmul_add<CONJ>(a.re, a.im, __ldg(coef32 + slot), __ldg(val + pos), parity);
     }
@@ -188,7 +180,7 @@ struct GatherF32C {
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         double re = a.re.value(), im = a.im.value();
         if (include_diag && (a.dre != 0.0 || a.dim != 0.0)) {
-            int64_t pos = find_key<W>(lookup, a.n, c);
+            int64_t pos = hash_find<W>(lookup, c);
             if (pos >= 0) {
                 float2 p = __ldg(val + pos);
                 re += a.dre * (double)p.x - a.dim * (double)p.y;
@@ -336,22 +328,22 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     KeyRows<W> src{walk.keys};
     if (a.prec == Prec::F64) {
         if (!a.adjoint) {
-            GatherF64<W, false> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
+            GatherF64<W, false> v{look.hash(), (const double2*)uval, walk_part.coef, diag.coef, a.out64,
                                   walk.first, nullptr, nullptr};
             QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         } else {
-            GatherF64<W, true> v{look.keys, look.count, (const double2*)uval, walk_part.coef, diag.coef, a.out64,
+            GatherF64<W, true> v{look.hash(), (const double2*)uval, walk_part.coef, diag.coef, a.out64,
                                  nullptr, walk.start, walk.perm};
             QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         }
     } else {
         if (!a.include_diag) diag.n = 0;
         if (!a.adjoint) {
-            GatherF32C<W, false> v{look.keys,  look.count, (const float2*)uval, walk_part.coef32, diag.coef,
+            GatherF32C<W, false> v{look.hash(), (const float2*)uval, walk_part.coef32, diag.coef,
                                    a.include_diag, a.out64, a.out32, walk.first, nullptr, nullptr};
             QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         } else {
-            GatherF32C<W, true> v{look.keys, look.count, (const float2*)uval, walk_part.coef32, diag.coef,
+            GatherF32C<W, true> v{look.hash(), (const float2*)uval, walk_part.coef32, diag.coef,
                                   a.include_diag, a.out64, a.out32, nullptr, walk.start, walk.perm};
             QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
         }

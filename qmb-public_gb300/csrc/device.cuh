@@ -88,20 +88,49 @@ __device__ __forceinline__ bool key_eq(const Key<W>& a, const Key<W>& b) {
     return e;
 }
 
-// Position of key among n sorted unique keys, or -1.
+// ---------------------------------------------------------------------------
+// open-addressing hash set over the unique keys of a row set
+//
+// slot = (32-bit fingerprint << 32) | index of the key among the unique keys,
+// all ones when empty; linear probing, load factor at most 1/2.
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kEmptySlot = ~0ull;
+
 template <int W>
-__device__ __forceinline__ int64_t find_key(const uint64_t* __restrict__ keys, int64_t n, const Key<W>& key) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        Key<W> m = load_key<W>(keys, mid);
-        if (key_cmp<W>(m, key) < 0) {
-            lo = mid + 1;
-        } else {
-            hi = mid;
-        }
+__host__ __device__ __forceinline__ uint64_t key_hash(const Key<W>& k) {
+    uint64_t h = 0x9E3779B97F4A7C15ull;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        h = (h ^ k.w[q]) * 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 31;
     }
-    if (lo < n && key_eq<W>(load_key<W>(keys, lo), key)) return lo;
+    h *= 0x94D049BB133111EBull;
+    h ^= h >> 29;
+    return h;
+}
+
+struct HashView {
+    const uint64_t* slots;
+    const uint64_t* keys;  // unique keys, n x W
+    uint64_t mask;         // slot count - 1 (a power of two minus one)
+};
+
+// Index of key among the unique keys, or -1.
+template <int W>
+__device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& key) {
+    const uint64_t hv = key_hash<W>(key);
+    const uint32_t fp = (uint32_t)(hv >> 32);
+    uint64_t i = hv & h.mask;
+    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
+        const uint64_t s = __ldg(h.slots + i);
+        if (s == kEmptySlot) return -1;
+        if ((uint32_t)(s >> 32) == fp) {
+            const int64_t idx = (int64_t)(uint32_t)s;
+            if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
+        }
+        i = (i + 1) & h.mask;
+    }
     return -1;
 }
 
@@ -213,13 +242,39 @@ struct ByteRows {
     }
 };
 
+// Test one row against every term of a staged tile: bit k of hit[k / 32] is
+// set when term k applies.  Full tiles are tested without bounds checks.
+template <int W>
+__device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, const Key<W>& c,
+                                          uint32_t (&hit)[kTermTile / 32]) {
+    if (count == kTermTile) {
+#pragma unroll
+        for (int w = 0; w < kTermTile / 32; ++w) {
+            uint32_t m = 0;
+#pragma unroll
+            for (int b = 0; b < 32; ++b) m |= (uint32_t)term_applies<W>(tile.m[32 * w + b], c) << b;
+            hit[w] = m;
+        }
+    } else {
+#pragma unroll
+        for (int w = 0; w < kTermTile / 32; ++w) {
+            uint32_t m = 0;
+            for (int b = 0; b < 32 && 32 * w + b < count; ++b) m |= (uint32_t)term_applies<W>(tile.m[32 * w + b], c) << b;
+            hit[w] = m;
+        }
+    }
+}
+
 // Visitor protocol:
 //   struct V { struct Acc; init(Acc&, int64_t row, const Key<W>&);
 //              visit(Acc&, const Key<W>& c, const Key<W>& image, int parity, int64_t slot);
 //              visit_diag(Acc&, const Key<W>& c, int parity, int64_t slot);
 //              finish(Acc&, int64_t row, const Key<W>&); }
 // Rows [0, *n_rows) (or [0, n_max) when n_rows is NULL) of src are visited;
-// off holds the terms that change a row, diag the ones that do not.
+// off holds the terms that change a row, diag the ones that do not.  Each
+// thread owns one row: it first tests its row against a whole tile of terms
+// (cheap, branch-free, all lanes reading the same term) and then visits only
+// the terms that applied.
 template <int W, class V, class Src>
 __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const int* __restrict__ n_rows,
                                                              int64_t n_max, PartView off, PartView diag) {
@@ -237,34 +292,29 @@ __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const
     }
     typename V::Acc acc;
     v.init(acc, row, c);
-    for (int64_t t0 = 0; t0 < off.n; t0 += kTermTile) {
-        int count = (int)(off.n - t0 < kTermTile ? off.n - t0 : kTermTile);
-        __syncthreads();
-        stage_tile<W>(tile, off, t0, count);
-        __syncthreads();
-        if (live) {
-            for (int k = 0; k < count; ++k) {
-                const uint64_t* t = tile.m[k];
-                if (term_applies<W>(t, c)) {
+    for (int part = 0; part < 2; ++part) {
+        const PartView& pv = part == 0 ? off : diag;
+        for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
+            const int count = (int)(pv.n - t0 < kTermTile ? pv.n - t0 : kTermTile);
+            __syncthreads();
+            stage_tile<W>(tile, pv, t0, count);
+            __syncthreads();
+            if (!live) continue;
+            uint32_t hit[kTermTile / 32];
+            test_tile<W>(tile, count, c, hit);
+#pragma unroll
+            for (int w = 0; w < kTermTile / 32; ++w) {
+                uint32_t m = hit[w];
+                while (m) {
+                    const int k = 32 * w + __ffs(m) - 1;
+                    m &= m - 1;
                     Key<W> img;
-                    int parity = term_image<W>(t, c, img);
-                    v.visit(acc, c, img, parity, t0 + k);
-                }
-            }
-        }
-    }
-    for (int64_t t0 = 0; t0 < diag.n; t0 += kTermTile) {
-        int count = (int)(diag.n - t0 < kTermTile ? diag.n - t0 : kTermTile);
-        __syncthreads();
-        stage_tile<W>(tile, diag, t0, count);
-        __syncthreads();
-        if (live) {
-            for (int k = 0; k < count; ++k) {
-                const uint64_t* t = tile.m[k];
-                if (term_applies<W>(t, c)) {
-                    Key<W> img;
-                    int parity = term_image<W>(t, c, img);
-                    v.visit_diag(acc, c, parity, t0 + k);
+                    const int parity = term_image<W>(tile.m[k], c, img);
+                    if (part == 0) {
+                        v.visit(acc, c, img, parity, t0 + k);
+                    } else {
+                        v.visit_diag(acc, c, parity, t0 + k);
+                    }
                 }
             }
         }
@@ -314,8 +364,11 @@ struct RowSet {
     int* count;             // device int: number of unique keys
     int32_t* head;
     int32_t* pos;
+    uint64_t* slots;        // hash set over the unique keys
+    uint64_t slot_mask;
     SortScratch sort;
     int64_t n;
+    HashView hash() const { return HashView{slots, keys, slot_mask}; }
 };
 
 template <int W>

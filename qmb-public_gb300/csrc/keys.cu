@@ -358,6 +358,25 @@ __global__ void compact_heads_kernel(const uint64_t* __restrict__ sorted, const 
 
 
 template <int W>
+__global__ void hash_insert_kernel(const uint64_t* __restrict__ keys, const int* __restrict__ count,
+                                   uint64_t* __restrict__ slots, uint64_t mask) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= *count) return;
+    Key<W> k = load_key<W>(keys, u);
+    uint64_t hv = key_hash<W>(k);
+    uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)u;
+    uint64_t i = hv & mask;
+    // the keys are unique and the table at most half full, so an empty slot
+    // is reached within mask + 1 probes
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+        unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long*>(slots + i),
+                                            (unsigned long long)kEmptySlot, (unsigned long long)entry);
+        if (prev == kEmptySlot) return;
+        i = (i + 1) & mask;
+    }
+}
+
+template <int W>
 RowSet take_rowset(Arena& ws, int64_t n) {
     RowSet out;
     uint64_t cap = (uint64_t)(n > 0 ? n : 1);
@@ -371,6 +390,10 @@ RowSet take_rowset(Arena& ws, int64_t n) {
     out.count = ws.take<int>(1);
     out.head = ws.take<int32_t>(cap);
     out.pos = ws.take<int32_t>(cap);
+    uint64_t slots = 64;
+    while (slots < 2 * cap) slots <<= 1;
+    out.slots = ws.take<uint64_t>(slots);
+    out.slot_mask = slots - 1;
     out.sort = take_sort_scratch<W>(ws, n);
     return out;
 }
@@ -380,6 +403,7 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     const int64_t n = out.n;
     if (n == 0) {
         QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
+        QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
         QMBX_LAUNCH_CHECK("set_int_kernel");
         return QMBX_OK;
     }
@@ -390,6 +414,8 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.sort.scan, s)) != QMBX_OK) return st;
     QMBX_KERNEL(kGroupKeys, s, compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
                                                                        out.keys, out.first, out.start, out.count));
+    QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
+    QMBX_KERNEL(kGroupKeys, s, hash_insert_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.keys, out.count, out.slots, out.slot_mask));
     QMBX_LAUNCH_CHECK("build_rowset");
     return QMBX_OK;
 }

@@ -50,8 +50,7 @@ struct RelativeArgs {
     const uint64_t* keys_i;  // packed configs_i, input order
     const double2* psi;
     int64_t n_i;
-    const uint64_t* excl;    // sorted unique exclude keys
-    const int* n_excl;
+    HashView excl;           // hash set over the unique exclude keys
     PartView off, diag;
     // pass 1
     unsigned long long* hist;
@@ -67,8 +66,8 @@ struct RelativeArgs {
 template <int W, bool EMIT>
 __device__ __forceinline__ void relative_candidate(const RelativeArgs& a, int* s_hist, const Key<W>& img, float norm,
                                                    float m, double2 cf, double2 p, int parity, int64_t orig,
-                                                   int64_t row, int64_t n_ex) {
-    if (find_key<W>(a.excl, n_ex, img) >= 0) return;
+                                                   int64_t row) {
+    if (hash_find<W>(a.excl, img) >= 0) return;
     int b = weight_bucket(__fmul_rn(norm, m));
     if (!EMIT) {
         atomicAdd(&s_hist[b], 1);
@@ -108,7 +107,6 @@ __global__ void __launch_bounds__(kThreads) relative_kernel(RelativeArgs a) {
         for (int q = 0; q < W; ++q) c.w[q] = 0;
     }
     const float m = (float)(p.x * p.x + p.y * p.y);
-    const int64_t n_ex = *a.n_excl;
     for (int part = 0; part < 2; ++part) {
         const PartView& pv = part == 0 ? a.off : a.diag;
         for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
@@ -116,18 +114,21 @@ __global__ void __launch_bounds__(kThreads) relative_kernel(RelativeArgs a) {
             __syncthreads();
             stage_tile<W>(tile, pv, t0, count);
             __syncthreads();
-            if (live) {
-                for (int k = 0; k < count; ++k) {
-                    const uint64_t* t = tile.m[k];
-                    if (term_applies<W>(t, c)) {
-                        Key<W> img;
-                        int parity = term_image<W>(t, c, img);
-                        int64_t slot = t0 + k;
-                        double2 cf = EMIT ? __ldg(pv.coef + slot) : make_double2(0.0, 0.0);
-                        int64_t orig = EMIT ? __ldg(pv.orig + slot) : 0;
-                        relative_candidate<W, EMIT>(a, s_hist, img, __ldg(pv.norm + slot), m, cf, p, parity, orig,
-                                                    row, n_ex);
-                    }
+            if (!live) continue;
+            uint32_t hit[kTermTile / 32];
+            test_tile<W>(tile, count, c, hit);
+#pragma unroll
+            for (int w = 0; w < kTermTile / 32; ++w) {
+                uint32_t mk = hit[w];
+                while (mk) {
+                    const int k = 32 * w + __ffs(mk) - 1;
+                    mk &= mk - 1;
+                    Key<W> img;
+                    int parity = term_image<W>(tile.m[k], c, img);
+                    int64_t slot = t0 + k;
+                    double2 cf = EMIT ? __ldg(pv.coef + slot) : make_double2(0.0, 0.0);
+                    int64_t orig = EMIT ? __ldg(pv.orig + slot) : 0;
+                    relative_candidate<W, EMIT>(a, s_hist, img, __ldg(pv.norm + slot), m, cf, p, parity, orig, row);
                 }
             }
         }
@@ -252,8 +253,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.keys_i = L.keys_i;
     r.psi = reinterpret_cast<const double2*>(a.psi_i);
     r.n_i = a.n_i;
-    r.excl = L.excl.keys;
-    r.n_excl = L.excl.count;
+    r.excl = L.excl.hash();
     r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
@@ -350,8 +350,7 @@ __global__ void es_factor_kernel(const double2* __restrict__ coef, const int32_t
 
 template <int W>
 struct SingleVisitor {
-    const uint64_t* set;
-    const int* n_set;
+    HashView set;
     const double* kf;
     const int32_t* orig;
     uint8_t* out;
@@ -360,12 +359,10 @@ struct SingleVisitor {
         double key;
         int32_t term;
         Key<W> best;
-        int64_t n;
     };
     __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
         a.key = -INFINITY;
         a.term = -1;
-        a.n = *n_set;
 #pragma unroll
         for (int q = 0; q < W; ++q) a.best.w[q] = 0;
     }
@@ -374,7 +371,7 @@ struct SingleVisitor {
         int32_t t = __ldg(orig + slot);
         bool better = a.term < 0 || key > a.key || (key == a.key && t < a.term);
         if (!better) return;
-        if (find_key<W>(set, a.n, img) >= 0) return;
+        if (hash_find<W>(set, img) >= 0) return;
         a.key = key;
         a.term = t;
         a.best = img;
@@ -417,7 +414,7 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     }
     PartView none = off;
     none.n = 0;
-    SingleVisitor<W> v{L.set.keys, L.set.count, L.kf, off.orig, out, h->n_qubytes};
+    SingleVisitor<W> v{L.set.hash(), L.kf, off.orig, out, h->n_qubytes};
     KeyRows<W> src{L.set.packed};
     QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
     QMBX_LAUNCH_CHECK("single_relative enumeration");
