@@ -100,7 +100,6 @@ constexpr uint64_t kEmptySlot = ~0ull;
 template <int W>
 __host__ __device__ __forceinline__ uint64_t key_hash(const Key<W>& k) {
     uint64_t h = 0x9E3779B97F4A7C15ull;
-#pragma unroll
     for (int q = 0; q < W; ++q) {
         h = (h ^ k.w[q]) * 0xBF58476D1CE4E5B9ull;
         h ^= h >> 31;
