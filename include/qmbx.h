@@ -88,6 +88,30 @@ int qmbx_apply_within(const void* table_host, const void* table_dev, const uint8
                       void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
 
 /*
+ * Allocation-free qmbx_apply_within (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory themselves or through this
+ * library: a host program that has given all device memory to its own pool
+ * and forbids further allocation, a latency-critical loop that cannot afford
+ * the implicit synchronisation of cudaMalloc/cudaFree, or a plain C caller
+ * without an allocator that does not want to size and keep a workspace.
+ * Same arguments and results as qmbx_apply_within minus the workspace: the
+ * scratch is a fixed device array of QMBX_STATIC_SCRATCH_BYTES inside this
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Inputs needing more scratch than that (qmbx_apply_within_workspace)
+ * are rejected with QMBX_ERR_ARGUMENT.  The array's device address is looked
+ * up on the first call made on each device (with that device current), so
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls whose work overlaps on the GPU race and must be serialised by
+ * the caller.  Calls no allocation routine.
+ */
+#define QMBX_STATIC_SCRATCH_BYTES (32ull << 20)
+
+int qmbx_apply_within_static(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                             const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                             int32_t same_configs, double* psi_j, qmbx_stream_t stream);
+
+/*
  * Adjoint of qmbx_apply_within (no counterpart in the reference): with the
  * same rows, out_i[i] = sum over t and j of conj(s * coef_t) * g_j[j], i.e.
  * H^dagger applied with the roles of the two row sets swapped.  Every row of

@@ -37,6 +37,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_table_counts": (ctypes.c_int, [_P, _PI64]),
     "qmbx_apply_within_workspace": (ctypes.c_int, [_P, _I64, _I64, _PU64]),
     "qmbx_apply_within": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P, _U64, _P]),
+    "qmbx_apply_within_static": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P]),
     "qmbx_apply_within_adjoint": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, _I32, _P, _P, _U64, _P]),
     "qmbx_apply_within_f32c": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
     "qmbx_apply_within_adjoint_f32c": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
