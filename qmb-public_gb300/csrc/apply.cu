@@ -57,6 +57,17 @@ struct CompSum {
         c = __fadd_rn(c, e);
     }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+    // Combine the lanes' pairs: two-sum of the leading parts, plain sum of the tails.
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            float s2 = __shfl_xor_sync(0xffffffffu, s, d);
+            float c2 = __shfl_xor_sync(0xffffffffu, c, d);
+            float e;
+            two_sum(s, s2, s, e);
+            c = __fadd_rn(c, __fadd_rn(c2, e));
+        }
+    }
 };
 
 // coef (hi/lo split, sign already folded) times psi, added to (re, im) with
@@ -93,7 +104,7 @@ __device__ __forceinline__ void comp_cmul_add(CompSum& re, CompSum& im, float4 c
 // adjoint (CONJ = true: sources walk the forward part, coef conjugated).
 // Values of the looked-up rows sit in val[u] for unique key u of lookup.
 template <int W, bool CONJ>
-struct GatherF64 {
+struct GatherF64 : VisitorBase {
     HashView lookup;         // hash set over the unique keys of the looked-up row set
     const double2* val;      // one amplitude per unique looked-up key
     const double2* coef;     // coefficients of the walked part
@@ -105,7 +116,7 @@ struct GatherF64 {
     struct Acc {
         double re, im, dre, dim;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const { a.re = a.im = a.dre = a.dim = 0.0; }
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.re = a.im = a.dre = a.dim = 0.0; }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
         int64_t pos = hash_find<W>(lookup, img);
         if (pos < 0) return;
@@ -127,6 +138,12 @@ struct GatherF64 {
         a.dre += parity ? -cf.x : cf.x;
         a.dim += parity ? -ci : ci;
     }
+    __device__ __forceinline__ void reduce(Acc& a) const {
+        a.re = warp_sum(a.re);
+        a.im = warp_sum(a.im);
+        a.dre = warp_sum(a.dre);
+        a.dim = warp_sum(a.dim);
+    }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         if (a.dre != 0.0 || a.dim != 0.0) {
             int64_t pos = hash_find<W>(lookup, c);
@@ -146,7 +163,7 @@ struct GatherF64 {
 };
 
 template <int W, bool CONJ>
-struct GatherF32C {
+struct GatherF32C : VisitorBase {
     HashView lookup;
     const float2* val;
     const float4* coef32;
@@ -161,7 +178,7 @@ struct GatherF32C {
         CompSum re, im;
         double dre, dim;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const {
         a.re.zero();
         a.im.zero();
         a.dre = a.dim = 0.0;
@@ -176,6 +193,12 @@ struct GatherF32C {
         double ci = CONJ ? -cf.y : cf.y;
         a.dre += parity ? -cf.x : cf.x;
         a.dim += parity ? -ci : ci;
+    }
+    __device__ __forceinline__ void reduce(Acc& a) const {
+        a.re.warp_reduce();
+        a.im.warp_reduce();
+        a.dre = warp_sum(a.dre);
+        a.dim = warp_sum(a.dim);
     }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         double re = a.re.value(), im = a.im.value();
@@ -202,23 +225,121 @@ struct GatherF32C {
 };
 
 template <int W>
-struct DiagonalF64 {
+struct DiagonalF64 : VisitorBase {
     const double2* dcoef;
     double2* out;
     struct Acc {
         double re, im;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const { a.re = a.im = 0.0; }
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.re = a.im = 0.0; }
     __device__ __forceinline__ void visit(Acc&, const Key<W>&, const Key<W>&, int, int64_t) const {}
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         double2 cf = __ldg(dcoef + slot);
         a.re += parity ? -cf.x : cf.x;
         a.im += parity ? -cf.y : cf.y;
     }
+    __device__ __forceinline__ void reduce(Acc& a) const {
+        a.re = warp_sum(a.re);
+        a.im = warp_sum(a.im);
+    }
     __device__ __forceinline__ void finish(Acc& a, int64_t row, const Key<W>&) const {
         out[row] = make_double2(a.re, a.im);
     }
 };
+
+// Scatter: the input-side rows are walked and every image found among the
+// output-side rows gets its contribution by an FP64 atomic add into acc[u].
+// FP32C forms the products in FP32 (exact two-products), FP64 otherwise.
+template <int W, bool CONJ, bool F32>
+struct Scatter : VisitorBase {
+    HashView lookup;        // output-side row set
+    const void* val;        // amplitude per unique walked key (double2, or float2 for F32)
+    const double2* coef;    // walked part, FP64
+    const float4* coef32;   // walked part, hi/lo FP32
+    const double2* dcoef;   // diagonal part
+    int include_diag;
+    double2* acc;           // per unique output-side key
+    struct Acc {
+        double2 p;
+        double dre, dim;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t row, const Key<W>&, int*) const {
+        if (F32) {
+            float2 q = __ldg(static_cast<const float2*>(val) + row);
+            a.p = make_double2((double)q.x, (double)q.y);
+        } else {
+            a.p = __ldg(static_cast<const double2*>(val) + row);
+        }
+        a.dre = a.dim = 0.0;
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
+        int64_t u = hash_find<W>(lookup, img);
+        if (u < 0) return;
+        double re, im;
+        if (F32) {
+            float4 cf = __ldg(coef32 + slot);
+            float2 p = make_float2((float)a.p.x, (float)a.p.y);
+            float chi = CONJ ? -cf.z : cf.z, cli = CONJ ? -cf.w : cf.w;
+            float x1, e1, x2, e2;
+            two_prod(cf.x, p.x, x1, e1);
+            two_prod(chi, p.y, x2, e2);
+            float lo = __fadd_rn(__fsub_rn(e1, e2), __fsub_rn(__fmul_rn(cf.y, p.x), __fmul_rn(cli, p.y)));
+            re = ((double)x1 - (double)x2) + (double)lo;
+            two_prod(cf.x, p.y, x1, e1);
+            two_prod(chi, p.x, x2, e2);
+            lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fmul_rn(cf.y, p.y), __fmul_rn(cli, p.x)));
+            im = ((double)x1 + (double)x2) + (double)lo;
+        } else {
+            double2 cf = __ldg(coef + slot);
+            double ci = CONJ ? -cf.y : cf.y;
+            re = cf.x * a.p.x - ci * a.p.y;
+            im = cf.x * a.p.y + ci * a.p.x;
+        }
+        if (parity) {
+            re = -re;
+            im = -im;
+        }
+        atomicAdd(&acc[u].x, re);
+        atomicAdd(&acc[u].y, im);
+    }
+    __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
+        double2 cf = __ldg(dcoef + slot);
+        double ci = CONJ ? -cf.y : cf.y;
+        a.dre += parity ? -cf.x : cf.x;
+        a.dim += parity ? -ci : ci;
+    }
+    __device__ __forceinline__ void reduce(Acc& a) const {
+        a.dre = warp_sum(a.dre);
+        a.dim = warp_sum(a.dim);
+    }
+    __device__ __forceinline__ void finish(Acc& a, int64_t, const Key<W>& c) const {
+        if (!include_diag || (a.dre == 0.0 && a.dim == 0.0)) return;
+        int64_t u = hash_find<W>(lookup, c);
+        if (u < 0) return;
+        atomicAdd(&acc[u].x, a.dre * a.p.x - a.dim * a.p.y);
+        atomicAdd(&acc[u].y, a.dre * a.p.y + a.dim * a.p.x);
+    }
+};
+
+// Scatter results: forward writes the first occurrence of each output key,
+// adjoint every row of its run.
+__global__ void scatter_finalize_kernel(const double2* __restrict__ acc, const int* __restrict__ count,
+                                        const int32_t* __restrict__ first, const int32_t* __restrict__ run_start,
+                                        const int32_t* __restrict__ run_perm, double2* __restrict__ out64,
+                                        float2* __restrict__ out32) {
+    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= *count) return;
+    double2 r = acc[u];
+    if (first) {
+        if (out64) out64[first[u]] = r;
+        if (out32) out32[first[u]] = make_float2((float)r.x, (float)r.y);
+    } else {
+        for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) {
+            if (out64) out64[run_perm[k]] = r;
+            if (out32) out32[run_perm[k]] = make_float2((float)r.x, (float)r.y);
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // per-unique-key amplitudes
@@ -275,81 +396,125 @@ struct ApplyArgs {
     int include_diag;
 };
 
+// Launch one enumeration over `walk` rows: the grouped kernel (warp per row)
+// when the walked part is large, the tiled kernel (thread per row) otherwise.
+template <int W, class V>
+int launch_walk(const V& v, const RowSet& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
+    KeyRows<W> src{walk.keys};
+    if (part.n >= kGroupedMinTerms) {
+        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+    } else {
+        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+    }
+    QMBX_LAUNCH_CHECK("apply_within enumeration");
+    return QMBX_OK;
+}
+
+// Forward maps amplitudes on configs_i (input side) to configs_j (output
+// side); the adjoint maps configs_j to configs_i.  Gather walks the output
+// side (daggered terms for the forward map), scatter walks the input side
+// (forward terms for the forward map) and adds into the output side with
+// atomics; the cheaper walk (fewer rows) is taken.
 template <int W>
 int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     const qmbx_table_header* h = header_of(a.table_host);
     const int nq = h->n_qubytes;
     RowSet rs_i = take_rowset<W>(ws, a.n_i);
     RowSet rs_j = a.same ? rs_i : take_rowset<W>(ws, a.n_j);
-    // amplitudes per unique key of the looked-up set
-    const int64_t n_lookup = a.adjoint ? a.n_j : a.n_i;
-    void* uval = a.prec == Prec::F64 ? (void*)ws.take<double2>((uint64_t)(n_lookup > 0 ? n_lookup : 1))
-                                     : (void*)ws.take<float2>((uint64_t)(n_lookup > 0 ? n_lookup : 1));
+    const int64_t n_in = a.adjoint ? a.n_j : a.n_i;
+    const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
+    void* uval = a.prec == Prec::F64 ? (void*)ws.take<double2>((uint64_t)(n_in > 0 ? n_in : 1))
+                                     : (void*)ws.take<float2>((uint64_t)(n_in > 0 ? n_in : 1));
+    double2* acc = ws.take<double2>((uint64_t)(n_out > 0 ? n_out : 1));
     if (ws.base == nullptr) return QMBX_OK;
     if (!ws.fits()) {
         return fail(QMBX_ERR_WORKSPACE, "workspace of %llu bytes is smaller than the %llu needed",
                     (unsigned long long)ws.cap, (unsigned long long)ws.used);
     }
-    const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
     if (n_out == 0) return QMBX_OK;
     if (a.out64) QMBX_CUDA_TRY(cudaMemsetAsync(a.out64, 0, (size_t)n_out * sizeof(double2), s));
     if (a.out32) QMBX_CUDA_TRY(cudaMemsetAsync(a.out32, 0, (size_t)n_out * sizeof(float2), s));
     int st;
     if ((st = build_rowset<W>(a.configs_i, nq, rs_i, s)) != QMBX_OK) return st;
     if (!a.same && (st = build_rowset<W>(a.configs_j, nq, rs_j, s)) != QMBX_OK) return st;
-    if (n_lookup == 0) return QMBX_OK;
+    if (n_in == 0) return QMBX_OK;
 
-    const RowSet& walk = a.adjoint ? rs_i : rs_j;   // rows whose values are computed
-    const RowSet& look = a.adjoint ? rs_j : rs_i;   // rows whose amplitudes are read
-    const unsigned grid_look = grid_for(n_lookup, kThreads);
+    const RowSet& in_set = a.adjoint ? rs_j : rs_i;
+    const RowSet& out_set = a.adjoint ? rs_i : rs_j;
+    // per-unique-key amplitude of the input side: the forward map sums repeated
+    // source rows, the adjoint reads the first occurrence of each target row
+    const unsigned grid_in = grid_for(n_in, kThreads);
     if (a.prec == Prec::F64) {
         const double2* in = static_cast<const double2*>(a.in);
         if (a.adjoint) {
-            QMBX_KERNEL(kGroupOther, s, first_value_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (double2*)uval));
+            QMBX_KERNEL(kGroupOther, s, first_value_kernel<double2><<<grid_in, kThreads, 0, s>>>(in, in_set.first, in_set.count, (double2*)uval));
         } else {
-            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<double2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
-                                                                  (double2*)uval));
+            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<double2><<<grid_in, kThreads, 0, s>>>(in, in_set.perm, in_set.start, in_set.count, (double2*)uval));
         }
     } else {
         const float2* in = static_cast<const float2*>(a.in);
         if (a.adjoint) {
-            QMBX_KERNEL(kGroupOther, s, first_value_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.first, look.count, (float2*)uval));
+            QMBX_KERNEL(kGroupOther, s, first_value_kernel<float2><<<grid_in, kThreads, 0, s>>>(in, in_set.first, in_set.count, (float2*)uval));
         } else {
-            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<float2><<<grid_look, kThreads, 0, s>>>(in, look.perm, look.start, look.count,
-                                                                 (float2*)uval));
+            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<float2><<<grid_in, kThreads, 0, s>>>(in, in_set.perm, in_set.start, in_set.count, (float2*)uval));
         }
     }
     QMBX_LAUNCH_CHECK("amplitude gather");
 
-    PartView walk_part = part_view(a.table_host, a.table_dev, a.adjoint ? QMBX_PART_FWD : QMBX_PART_ADJ);
+    PartView fwd = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
+    PartView adj = part_view(a.table_host, a.table_dev, QMBX_PART_ADJ);
     PartView diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
-    const int64_t n_walk = walk.n;
-    const unsigned grid = grid_for(n_walk, kThreads);
-    KeyRows<W> src{walk.keys};
+    const bool include_diag = a.prec == Prec::F64 || a.include_diag;
+    if (!include_diag) diag.n = 0;
+    const bool scatter = !a.same && 2 * n_in < n_out;
+    if (scatter) {
+        // walk the input side: forward terms for the forward map, daggered
+        // terms (conjugated) for the adjoint
+        const PartView& part = a.adjoint ? adj : fwd;
+        QMBX_CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)n_out * sizeof(double2), s));
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                Scatter<W, true, false> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, 1, acc};
+                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+            } else {
+                Scatter<W, false, false> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, 1, acc};
+                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+            }
+        } else {
+            if (a.adjoint) {
+                Scatter<W, true, true> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, include_diag, acc};
+                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+            } else {
+                Scatter<W, false, true> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, include_diag, acc};
+                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+            }
+        }
+        QMBX_KERNEL(kGroupOther, s, scatter_finalize_kernel<<<grid_for(n_out, kThreads), kThreads, 0, s>>>(
+            acc, out_set.count, a.adjoint ? nullptr : out_set.first, out_set.start, out_set.perm, a.out64, a.out32));
+        QMBX_LAUNCH_CHECK("scatter_finalize_kernel");
+        return QMBX_OK;
+    }
+    // gather: walk the output side with daggered terms for the forward map,
+    // forward terms (conjugated) for the adjoint
+    const PartView& part = a.adjoint ? fwd : adj;
     if (a.prec == Prec::F64) {
         if (!a.adjoint) {
-            GatherF64<W, false> v{look.hash(), (const double2*)uval, walk_part.coef, diag.coef, a.out64,
-                                  walk.first, nullptr, nullptr};
-            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
-        } else {
-            GatherF64<W, true> v{look.hash(), (const double2*)uval, walk_part.coef, diag.coef, a.out64,
-                                 nullptr, walk.start, walk.perm};
-            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
+            GatherF64<W, false> v{{}, in_set.hash(), (const double2*)uval, part.coef, diag.coef, a.out64, out_set.first,
+                                  nullptr, nullptr};
+            return launch_walk<W>(v, out_set, part, diag, s);
         }
-    } else {
-        if (!a.include_diag) diag.n = 0;
-        if (!a.adjoint) {
-            GatherF32C<W, false> v{look.hash(), (const float2*)uval, walk_part.coef32, diag.coef,
-                                   a.include_diag, a.out64, a.out32, walk.first, nullptr, nullptr};
-            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
-        } else {
-            GatherF32C<W, true> v{look.hash(), (const float2*)uval, walk_part.coef32, diag.coef,
-                                  a.include_diag, a.out64, a.out32, nullptr, walk.start, walk.perm};
-            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid, kThreads, 0, s>>>(v, src, walk.count, n_walk, walk_part, diag));
-        }
+        GatherF64<W, true> v{{}, in_set.hash(), (const double2*)uval, part.coef, diag.coef, a.out64, nullptr,
+                             out_set.start, out_set.perm};
+        return launch_walk<W>(v, out_set, part, diag, s);
     }
-    QMBX_LAUNCH_CHECK("apply_within enumeration");
-    return QMBX_OK;
+    if (!a.adjoint) {
+        GatherF32C<W, false> v{{}, in_set.hash(), (const float2*)uval, part.coef32, diag.coef, a.include_diag, a.out64,
+                               a.out32, out_set.first, nullptr, nullptr};
+        return launch_walk<W>(v, out_set, part, diag, s);
+    }
+    GatherF32C<W, true> v{{}, in_set.hash(), (const float2*)uval, part.coef32, diag.coef, a.include_diag, a.out64,
+                          a.out32, nullptr, out_set.start, out_set.perm};
+    return launch_walk<W>(v, out_set, part, diag, s);
 }
 
 int dispatch_apply(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
@@ -403,9 +568,13 @@ int diagonal_impl(const void* table_host, const void* table_dev, const uint8_t* 
     PartView none = part_view(table_host, table_dev, QMBX_PART_DIAG);
     none.n = 0;
     PartView diag = part_view(table_host, table_dev, QMBX_PART_DIAG);
-    DiagonalF64<W> v{diag.coef, out};
+    DiagonalF64<W> v{{}, diag.coef, out};
     ByteRows<W> src{configs, h->n_qubytes};
-    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));
+    if (diag.n >= kGroupedMinTerms) {
+        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));
+    } else {
+        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));
+    }
     QMBX_LAUNCH_CHECK("diagonal_term enumeration");
     return QMBX_OK;
 }

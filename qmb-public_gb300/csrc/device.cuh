@@ -144,7 +144,11 @@ struct PartView {
     const float4* coef32;
     const int32_t* orig;
     const float* norm;
+    const int2* groups;        // [start, end) of every pivot group
+    const uint64_t* single_ne; // [W]
+    const uint64_t* pair_ne;   // [64W][W]
     int64_t n;
+    int wide;                  // groups are large: walk each with lanes over its terms
 };
 
 inline PartView part_view(const void* table_host, const void* table_dev, int which) {
@@ -158,7 +162,11 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
     v.coef32 = reinterpret_cast<const float4*>(base + p.off_coef32);
     v.orig = reinterpret_cast<const int32_t*>(base + p.off_orig);
     v.norm = reinterpret_cast<const float*>(base + p.off_norm);
+    v.groups = reinterpret_cast<const int2*>(base + p.off_groups);
+    v.single_ne = reinterpret_cast<const uint64_t*>(base + p.off_single_ne);
+    v.pair_ne = reinterpret_cast<const uint64_t*>(base + p.off_pair_ne);
     v.n = p.n;
+    v.wide = p.wide_groups;
     return v;
 }
 
@@ -264,8 +272,16 @@ __device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, co
     }
 }
 
+// Defaults for the optional parts of the visitor protocol: no shared memory,
+// no per-block set-up or flush.
+struct VisitorBase {
+    static constexpr int kShared = 0;
+    __device__ __forceinline__ void block_init(int*) const {}
+    __device__ __forceinline__ void block_flush(int*) const {}
+};
+
 // Visitor protocol:
-//   struct V { struct Acc; init(Acc&, int64_t row, const Key<W>&);
+//   struct V : VisitorBase { struct Acc; init(Acc&, int64_t row, const Key<W>&, int* shared);
 //              visit(Acc&, const Key<W>& c, const Key<W>& image, int parity, int64_t slot);
 //              visit_diag(Acc&, const Key<W>& c, int parity, int64_t slot);
 //              finish(Acc&, int64_t row, const Key<W>&); }
@@ -289,8 +305,11 @@ __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const
 #pragma unroll
         for (int q = 0; q < W; ++q) c.w[q] = 0;
     }
+    __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
+    v.block_init(sh);
+    __syncthreads();
     typename V::Acc acc;
-    v.init(acc, row, c);
+    v.init(acc, row, c, sh);
     for (int part = 0; part < 2; ++part) {
         const PartView& pv = part == 0 ? off : diag;
         for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
@@ -319,6 +338,144 @@ __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const
         }
     }
     if (live) v.finish(acc, row, c);
+    __syncthreads();
+    v.block_flush(sh);
+}
+
+// ---------------------------------------------------------------------------
+// the grouped enumeration kernel: one warp per row, visiting only the pivot
+// groups whose sites the row occupies (see format.h).  Large groups are
+// walked with the lanes over their terms (coalesced term loads); small ones
+// with the lanes over groups.  Visitors additionally provide
+// reduce(Acc&) (warp-wide, every lane ends with the total) and finish() is
+// called by lane 0.  Rows are taken grid-stride, so the grid can be sized to
+// the machine.
+// ---------------------------------------------------------------------------
+
+constexpr int kWarpsPerBlock = kThreads / 32;
+
+// Parts with at least this many terms are walked by grouped_kernel.
+constexpr int64_t kGroupedMinTerms = 2048;
+
+template <int W, bool DIAG, class V>
+__device__ __forceinline__ void visit_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
+                                           int64_t t) {
+    const uint64_t* test = pv.test + t * 2 * W;
+    uint64_t bad = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ __ldg(test + 2 * q + 1)) & __ldg(test + 2 * q);
+    if (bad) return;
+    const uint64_t* ap = pv.apply + t * 2 * W;
+    Key<W> img;
+    int par = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        img.w[q] = c.w[q] ^ __ldg(ap + 2 * q);
+        par += __popcll(c.w[q] & __ldg(ap + 2 * q + 1));
+    }
+    if (DIAG) {
+        v.visit_diag(acc, c, par & 1, t);
+    } else {
+        v.visit(acc, c, img, par & 1, t);
+    }
+}
+
+// Walk one group: lanes over its terms.
+template <int W, bool DIAG, class V>
+__device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& acc, const Key<W>& c,
+                                                 const PartView& pv, int64_t g, int lane) {
+    const int2 se = __ldg(pv.groups + g);
+    for (int64_t t = se.x + lane; t < se.y; t += 32) visit_term<W, DIAG>(v, acc, c, pv, t);
+}
+
+// Walk one group entirely in this lane.
+template <int W, bool DIAG, class V>
+__device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& acc, const Key<W>& c,
+                                                  const PartView& pv, int64_t g) {
+    const int2 se = __ldg(pv.groups + g);
+    for (int64_t t = se.x; t < se.y; ++t) visit_term<W, DIAG>(v, acc, c, pv, t);
+}
+
+// Visit the groups named by the set bits of a 64-bit mask (key positions
+// 64 * word + bit), as single groups (second < 0) or pair groups with first.
+template <int W, bool DIAG, class V>
+__device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
+                                          uint64_t bits, int word, int first, int lane) {
+    if (pv.wide) {
+        while (bits) {
+            const int b = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const int kp = 64 * word + b;
+            const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
+            walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane);
+        }
+    } else {
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const uint32_t chunk = (uint32_t)(bits >> (32 * half));
+            if ((chunk >> lane) & 1u) {
+                const int kp = 64 * word + 32 * half + lane;
+                const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
+                walk_group_serial<W, DIAG>(v, acc, c, pv, g);
+            }
+        }
+    }
+}
+
+template <int W, bool DIAG, class V>
+__device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
+                                          int lane) {
+    if (pv.n == 0) return;
+    walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane);
+#pragma unroll
+    for (int q = 0; q < W; ++q) walk_mask<W, DIAG>(v, acc, c, pv, c.w[q] & __ldg(pv.single_ne + q), q, -1, lane);
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        uint64_t occ = c.w[q];
+        while (occ) {
+            const int b = __ffsll((long long)occ) - 1;
+            occ &= occ - 1;
+            const int kp = 64 * q + b;
+            const uint64_t* pn = pv.pair_ne + (int64_t)kp * W;
+#pragma unroll
+            for (int r = 0; r < W; ++r) {
+                if (r < q) continue;  // partners sit at higher key positions
+                walk_mask<W, DIAG>(v, acc, c, pv, c.w[r] & __ldg(pn + r), r, kp, lane);
+            }
+        }
+    }
+}
+
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const int* __restrict__ n_rows,
+                                                           int64_t n_max, PartView off, PartView diag) {
+    __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
+    v.block_init(sh);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
+    const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t row = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); row < n; row += stride) {
+        const Key<W> c = src.get(row);
+        typename V::Acc acc;
+        v.init(acc, row, c, sh);
+        walk_part<W, false>(v, acc, c, off, lane);
+        walk_part<W, true>(v, acc, c, diag, lane);
+        v.reduce(acc);
+        if (lane == 0) v.finish(acc, row, c);
+    }
+    __syncthreads();
+    v.block_flush(sh);
+}
+
+// Grid for grouped_kernel: enough warps for every row, at most a few waves.
+int grouped_grid(int64_t n_rows);
+
+// Lane-sum of a double across the warp (butterfly: every lane gets the total).
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(0xffffffffu, x, d);
+    return x;
 }
 
 // ---------------------------------------------------------------------------

@@ -23,12 +23,23 @@
 // the diagonal part (terms whose flip mask is empty).  Terms that can never
 // apply (an operator writing the value a previous operator of the same term
 // left) are dropped.
+//
+// Within each part the terms are grouped by a pivot taken from the sites
+// they require occupied (bits of mask & val), numbered by key position
+// kp = word * 64 + bit: the two lowest such positions (p < q) give the pair
+// group 1 + 64W + q(q-1)/2 + p, a single one gives the single group 1 + p,
+// none gives group 0.  A row can only be acted on by terms whose pivot sites
+// it occupies, so a walk over a row visits group 0, the single groups of its
+// occupied positions and the pair groups of its occupied pairs, nothing else.
+// Terms are stored sorted by group (stable in input order); groups[g] holds
+// [start, end); single_ne marks non-empty single groups and pair_ne[p] the
+// positions q > p whose pair group is non-empty.
 #pragma once
 
 #include <stdint.h>
 
 #define QMBX_MAGIC 0x58424D51u  // "QMBX"
-#define QMBX_TABLE_VERSION 2u
+#define QMBX_TABLE_VERSION 3u
 #define QMBX_MAX_WORDS 4
 #define QMBX_ALIGN 256
 
@@ -42,6 +53,13 @@ struct qmbx_table_part {
     uint64_t off_coef32;  // float[n][4]    (re_hi, re_lo, im_hi, im_lo)
     uint64_t off_orig;    // int32[n]       index of the term in the input table
     uint64_t off_norm;    // float[n]       |coef|^2 rounded to FP32
+    uint64_t off_groups;  // int32[n_groups][2]  [start, end) of each group
+    uint64_t off_single_ne;  // uint64[W]       non-empty single groups by key position
+    uint64_t off_pair_ne;    // uint64[64W][W]  for position p: positions q > p with a non-empty pair group
+    int64_t n_groups;        // 1 + 64W + 64W(64W-1)/2
+    int64_t n_nonempty;      // groups holding at least one term
+    int32_t wide_groups;     // 1 when non-empty groups hold 8 or more terms on average
+    int32_t reserved;
 };
 
 struct qmbx_table_header {
@@ -60,4 +78,21 @@ struct qmbx_table_header {
 #ifdef __cplusplus
 static inline int qmbx_keyword(int s) { return s >> 6; }
 static inline int qmbx_keybit(int s) { return (7 - ((s >> 3) & 7)) * 8 + (s & 7); }
+static inline int64_t qmbx_group_count(int words) {
+    int64_t p = 64 * (int64_t)words;
+    return 1 + p + p * (p - 1) / 2;
+}
+#endif
+
+#ifdef __CUDACC__
+#define QMBX_HD __host__ __device__
+#else
+#define QMBX_HD
+#endif
+
+#ifdef __cplusplus
+static inline QMBX_HD int64_t qmbx_single_group(int kp) { return 1 + kp; }
+static inline QMBX_HD int64_t qmbx_pair_group(int words, int p, int q) {
+    return 1 + 64 * (int64_t)words + (int64_t)q * (q - 1) / 2 + p;
+}
 #endif

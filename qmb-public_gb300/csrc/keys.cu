@@ -435,3 +435,22 @@ QMBX_INSTANTIATE_KEYS(3)
 QMBX_INSTANTIATE_KEYS(4)
 
 }  // namespace qmbx
+
+namespace qmbx {
+
+int grouped_grid(int64_t n_rows) {
+    static int sms[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    if (sms[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
+        sms[dev] = v;
+    }
+    int64_t want = (n_rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    int64_t cap = (int64_t)sms[dev] * 16;
+    if (want > cap) want = cap;
+    return (int)(want > 0 ? want : 1);
+}
+
+}  // namespace qmbx

@@ -44,11 +44,12 @@ __device__ __forceinline__ double exact_weight(double2 cf, double2 p, int parity
     return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
 }
 
-// The histogram and emission passes need per-row data (|psi|^2) and a shared
-// histogram, so they use their own kernel rather than enumerate_kernel.
+// The histogram (EMIT = false) and emission (EMIT = true) passes as
+// visitors of the enumeration kernels.  Every (term, row) image that is not
+// an excluded row is a candidate record; diagonal terms produce the row
+// itself.  The histogram lives in shared memory and is flushed once per block.
 struct RelativeArgs {
-    const uint64_t* keys_i;  // packed configs_i, input order
-    const double2* psi;
+    const double2* psi;      // configs_i amplitudes, input order
     int64_t n_i;
     HashView excl;           // hash set over the unique exclude keys
     PartView off, diag;
@@ -64,82 +65,78 @@ struct RelativeArgs {
 };
 
 template <int W, bool EMIT>
-__device__ __forceinline__ void relative_candidate(const RelativeArgs& a, int* s_hist, const Key<W>& img, float norm,
-                                                   float m, double2 cf, double2 p, int parity, int64_t orig,
-                                                   int64_t row) {
-    if (hash_find<W>(a.excl, img) >= 0) return;
-    int b = weight_bucket(__fmul_rn(norm, m));
-    if (!EMIT) {
-        atomicAdd(&s_hist[b], 1);
-        return;
+struct RelativeVisitor : VisitorBase {
+    RelativeArgs a;
+    static constexpr int kShared = EMIT ? 0 : kBuckets;
+    struct Acc {
+        double2 p;
+        float m;
+        int64_t row;
+        int* hist;
+    };
+    __device__ __forceinline__ void block_init(int* sh) const {
+        if (!EMIT) {
+            for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) sh[k] = 0;
+        }
     }
-    if (b < a.emit_from) return;
-    double w = exact_weight(cf, p, parity);
-    if (w == 0.0) return;
-    unsigned long long slot = atomicAdd(a.n_emit, 1ull);
-    if ((int64_t)slot >= a.cap_emit) {
-        *a.overflow = 1;
-        return;
-    }
-    uint64_t order = (uint64_t)orig * (uint64_t)a.n_i + (uint64_t)row;
-    a.emit_rank[2 * slot + 0] = ~(uint64_t)__double_as_longlong(w);
-    a.emit_rank[2 * slot + 1] = ~order;
-#pragma unroll
-    for (int q = 0; q < W; ++q) a.emit_keys[slot * W + q] = img.w[q];
-}
-
-template <int W, bool EMIT>
-__global__ void __launch_bounds__(kThreads) relative_kernel(RelativeArgs a) {
-    __shared__ TermTile<W> tile;
-    __shared__ int s_hist[EMIT ? 1 : kBuckets];
-    if (!EMIT) {
-        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) s_hist[k] = 0;
-    }
-    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = row < a.n_i;
-    Key<W> c;
-    double2 p = make_double2(0.0, 0.0);
-    if (live) {
-        c = load_key<W>(a.keys_i, row);
-        p = a.psi[row];
-    } else {
-#pragma unroll
-        for (int q = 0; q < W; ++q) c.w[q] = 0;
-    }
-    const float m = (float)(p.x * p.x + p.y * p.y);
-    for (int part = 0; part < 2; ++part) {
-        const PartView& pv = part == 0 ? a.off : a.diag;
-        for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
-            int count = (int)(pv.n - t0 < kTermTile ? pv.n - t0 : kTermTile);
-            __syncthreads();
-            stage_tile<W>(tile, pv, t0, count);
-            __syncthreads();
-            if (!live) continue;
-            uint32_t hit[kTermTile / 32];
-            test_tile<W>(tile, count, c, hit);
-#pragma unroll
-            for (int w = 0; w < kTermTile / 32; ++w) {
-                uint32_t mk = hit[w];
-                while (mk) {
-                    const int k = 32 * w + __ffs(mk) - 1;
-                    mk &= mk - 1;
-                    Key<W> img;
-                    int parity = term_image<W>(tile.m[k], c, img);
-                    int64_t slot = t0 + k;
-                    double2 cf = EMIT ? __ldg(pv.coef + slot) : make_double2(0.0, 0.0);
-                    int64_t orig = EMIT ? __ldg(pv.orig + slot) : 0;
-                    relative_candidate<W, EMIT>(a, s_hist, img, __ldg(pv.norm + slot), m, cf, p, parity, orig, row);
-                }
+    __device__ __forceinline__ void block_flush(int* sh) const {
+        if (!EMIT) {
+            for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
+                int v = sh[k];
+                if (v) atomicAdd(a.hist + k, (unsigned long long)v);
             }
         }
     }
-    if (!EMIT) {
-        __syncthreads();
-        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
-            int v = s_hist[k];
-            if (v) atomicAdd(a.hist + k, (unsigned long long)v);
-        }
+    __device__ __forceinline__ void init(Acc& acc, int64_t row, const Key<W>&, int* sh) const {
+        acc.p = __ldg(a.psi + row);
+        acc.m = (float)(acc.p.x * acc.p.x + acc.p.y * acc.p.y);
+        acc.row = row;
+        acc.hist = sh;
     }
+    __device__ __forceinline__ void candidate(Acc& acc, const Key<W>& img, const PartView& pv, int parity,
+                                              int64_t slot) const {
+        if (hash_find<W>(a.excl, img) >= 0) return;
+        const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
+        if (!EMIT) {
+            atomicAdd(&acc.hist[b], 1);
+            return;
+        }
+        if (b < a.emit_from) return;
+        const double w = exact_weight(__ldg(pv.coef + slot), acc.p, parity);
+        if (w == 0.0) return;
+        const unsigned long long at = atomicAdd(a.n_emit, 1ull);
+        if ((int64_t)at >= a.cap_emit) {
+            *a.overflow = 1;
+            return;
+        }
+        const uint64_t order = (uint64_t)__ldg(pv.orig + slot) * (uint64_t)a.n_i + (uint64_t)acc.row;
+        a.emit_rank[2 * at + 0] = ~(uint64_t)__double_as_longlong(w);
+        a.emit_rank[2 * at + 1] = ~order;
+#pragma unroll
+        for (int q = 0; q < W; ++q) a.emit_keys[at * W + q] = img.w[q];
+    }
+    __device__ __forceinline__ void visit(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
+        candidate(acc, img, a.off, parity, slot);
+    }
+    __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
+        candidate(acc, c, a.diag, parity, slot);
+    }
+    __device__ __forceinline__ void reduce(Acc&) const {}
+    __device__ __forceinline__ void finish(Acc&, int64_t, const Key<W>&) const {}
+};
+
+template <int W, bool EMIT>
+int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, cudaStream_t s) {
+    RelativeVisitor<W, EMIT> v;
+    v.a = r;
+    KeyRows<W> src{keys_i};
+    if (r.off.n >= kGroupedMinTerms) {
+        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
+    } else {
+        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
+    }
+    QMBX_LAUNCH_CHECK(EMIT ? "find_relative emission pass" : "find_relative histogram pass");
+    return QMBX_OK;
 }
 
 // Gather the keys of the first `keep` ranked records.
@@ -250,16 +247,13 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
 
     RelativeArgs r{};
-    r.keys_i = L.keys_i;
     r.psi = reinterpret_cast<const double2*>(a.psi_i);
     r.n_i = a.n_i;
     r.excl = L.excl.hash();
     r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
-    const unsigned grid = grid_for(a.n_i, kThreads);
-    QMBX_KERNEL(kGroupEnumerate, s, relative_kernel<W, false><<<grid, kThreads, 0, s>>>(r));
-    QMBX_LAUNCH_CHECK("find_relative histogram pass");
+    if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
 
     std::vector<unsigned long long> hist(kBuckets);
     QMBX_CUDA_TRY(cudaMemcpyAsync(hist.data(), L.hist, kBuckets * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
@@ -292,8 +286,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.emit_rank = L.emit_rank;
     r.emit_keys = L.emit_keys;
     r.overflow = L.overflow;
-    QMBX_KERNEL(kGroupEnumerate, s, relative_kernel<W, true><<<grid, kThreads, 0, s>>>(r));
-    QMBX_LAUNCH_CHECK("find_relative emission pass");
+    if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
     unsigned long long n_emit = 0;
     int overflow = 0;
     QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
@@ -349,7 +342,7 @@ __global__ void es_factor_kernel(const double2* __restrict__ coef, const int32_t
 }
 
 template <int W>
-struct SingleVisitor {
+struct SingleVisitor : VisitorBase {
     HashView set;
     const double* kf;
     const int32_t* orig;
@@ -360,7 +353,7 @@ struct SingleVisitor {
         int32_t term;
         Key<W> best;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&) const {
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const {
         a.key = -INFINITY;
         a.term = -1;
 #pragma unroll
@@ -377,6 +370,23 @@ struct SingleVisitor {
         a.best = img;
     }
     __device__ __forceinline__ void visit_diag(Acc&, const Key<W>&, int, int64_t) const {}
+    // warp argmax of (key, lowest term) carrying the image
+    __device__ __forceinline__ void reduce(Acc& a) const {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            double k2 = __shfl_xor_sync(0xffffffffu, a.key, d);
+            int32_t t2 = __shfl_xor_sync(0xffffffffu, a.term, d);
+            Key<W> b2;
+#pragma unroll
+            for (int q = 0; q < W; ++q) b2.w[q] = __shfl_xor_sync(0xffffffffu, a.best.w[q], d);
+            bool take = t2 >= 0 && (a.term < 0 || k2 > a.key || (k2 == a.key && t2 < a.term));
+            if (take) {
+                a.key = k2;
+                a.term = t2;
+                a.best = b2;
+            }
+        }
+    }
     __device__ __forceinline__ void finish(Acc& a, int64_t row, const Key<W>&) const {
         uint8_t* r = out + row * nq;
         for (int b = 0; b < nq; ++b) r[b] = (uint8_t)(a.best.w[b >> 3] >> (8 * (7 - (b & 7))));
@@ -414,9 +424,13 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     }
     PartView none = off;
     none.n = 0;
-    SingleVisitor<W> v{L.set.hash(), L.kf, off.orig, out, h->n_qubytes};
+    SingleVisitor<W> v{{}, L.set.hash(), L.kf, off.orig, out, h->n_qubytes};
     KeyRows<W> src{L.set.packed};
-    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
+    if (off.n >= kGroupedMinTerms) {
+        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
+    } else {
+        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
+    }
     QMBX_LAUNCH_CHECK("single_relative enumeration");
     return QMBX_OK;
 }

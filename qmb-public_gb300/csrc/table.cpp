@@ -141,6 +141,7 @@ struct Layout {
 
 void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     p.n = n;
+    p.n_groups = qmbx_group_count(words);
     uint64_t un = (uint64_t)n;
     p.off_test = cursor;
     cursor = align_up(cursor + un * 2 * words * 8);
@@ -154,6 +155,69 @@ void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     cursor = align_up(cursor + un * 4);
     p.off_norm = cursor;
     cursor = align_up(cursor + un * 4);
+    p.off_groups = cursor;
+    cursor = align_up(cursor + (uint64_t)p.n_groups * 8);
+    p.off_single_ne = cursor;
+    cursor = align_up(cursor + (uint64_t)words * 8);
+    p.off_pair_ne = cursor;
+    cursor = align_up(cursor + (uint64_t)64 * words * words * 8);
+}
+
+// Pivot group of a compiled term (see format.h).
+int64_t group_of(const Compiled& c, int words) {
+    int first = -1, second = -1;
+    for (int w = 0; w < words && second < 0; ++w) {
+        uint64_t req = c.mask[w] & c.val[w];
+        while (req && second < 0) {
+            int b = __builtin_ctzll(req);
+            req &= req - 1;
+            int kp = 64 * w + b;
+            if (first < 0) {
+                first = kp;
+            } else {
+                second = kp;
+            }
+        }
+    }
+    if (second >= 0) return qmbx_pair_group(words, first, second);
+    if (first >= 0) return qmbx_single_group(first);
+    return 0;
+}
+
+// Counting sort of one part's terms by group: fills groups[g] = [start, end),
+// the non-empty masks and the per-term destination slot.
+void group_part(char* blob, qmbx_table_part& p, int words, const std::vector<int64_t>& gid,
+                std::vector<int64_t>& dest) {
+    const int64_t G = p.n_groups;
+    std::vector<int64_t> count((size_t)G + 1, 0);
+    for (int64_t g : gid) ++count[(size_t)g + 1];
+    for (int64_t g = 0; g < G; ++g) count[(size_t)g + 1] += count[(size_t)g];
+    int32_t* groups = reinterpret_cast<int32_t*>(blob + p.off_groups);
+    uint64_t* single_ne = reinterpret_cast<uint64_t*>(blob + p.off_single_ne);
+    uint64_t* pair_ne = reinterpret_cast<uint64_t*>(blob + p.off_pair_ne);
+    int64_t nonempty = 0;
+    const int P = 64 * words;
+    for (int64_t g = 0; g < G; ++g) {
+        groups[2 * g + 0] = (int32_t)count[(size_t)g];
+        groups[2 * g + 1] = (int32_t)count[(size_t)g + 1];
+        if (count[(size_t)g + 1] == count[(size_t)g]) continue;
+        ++nonempty;
+        if (g >= 1 && g <= P) {
+            int kp = (int)(g - 1);
+            single_ne[kp >> 6] |= 1ull << (kp & 63);
+        } else if (g > P) {
+            int64_t r = g - 1 - P;  // q(q-1)/2 + p
+            int q = 1;
+            while ((int64_t)(q + 1) * q / 2 <= r) ++q;
+            int pp = (int)(r - (int64_t)q * (q - 1) / 2);
+            pair_ne[(size_t)pp * words + (q >> 6)] |= 1ull << (q & 63);
+        }
+    }
+    p.n_nonempty = nonempty;
+    p.wide_groups = (nonempty > 0 && p.n >= 8 * nonempty) ? 1 : 0;
+    dest.resize(gid.size());
+    std::vector<int64_t> cursor(count.begin(), count.end() - 1);
+    for (size_t k = 0; k < gid.size(); ++k) dest[k] = cursor[(size_t)gid[k]]++;
 }
 
 qmbx_table_header make_header(int64_t n_terms, int32_t n_qubytes, int32_t particle_cut, int64_t n_off, int64_t n_diag) {
@@ -255,22 +319,39 @@ extern "C" int qmbx_table_build(const int16_t* site, const uint8_t* kind, const 
     }
     char* out = static_cast<char*>(blob);
     std::memset(out, 0, h.total_bytes);
-    std::memcpy(out, &h, sizeof(h));
     Below below(h.n_sites, h.n_words);
     bool fermi = particle_cut == 1;
+    const int words = h.n_words;
+    // pass 1: group of every live term in each part
+    std::vector<int64_t> gid[QMBX_PARTS];
+    for (int64_t t = 0; t < n_terms; ++t) {
+        Compiled c = compile_term(site + 4 * t, kind + 4 * t, fermi, false, below);
+        if (!c.live) continue;
+        if (c.diagonal()) {
+            gid[QMBX_PART_DIAG].push_back(group_of(c, words));
+        } else {
+            gid[QMBX_PART_FWD].push_back(group_of(c, words));
+            Compiled a = compile_term(site + 4 * t, kind + 4 * t, fermi, true, below);
+            gid[QMBX_PART_ADJ].push_back(group_of(a, words));
+        }
+    }
+    std::vector<int64_t> dest[QMBX_PARTS];
+    for (int part = 0; part < QMBX_PARTS; ++part) group_part(out, h.part[part], words, gid[part], dest[part]);
+    // pass 2: write every term at its grouped position
     int64_t k_off = 0, k_diag = 0;
     for (int64_t t = 0; t < n_terms; ++t) {
         Compiled c = compile_term(site + 4 * t, kind + 4 * t, fermi, false, below);
         if (!c.live) continue;
         if (c.diagonal()) {
-            write_term(out, h.part[QMBX_PART_DIAG], h.n_words, k_diag++, c, coef + 2 * t, t);
+            write_term(out, h.part[QMBX_PART_DIAG], words, dest[QMBX_PART_DIAG][(size_t)k_diag++], c, coef + 2 * t, t);
         } else {
-            write_term(out, h.part[QMBX_PART_FWD], h.n_words, k_off, c, coef + 2 * t, t);
+            write_term(out, h.part[QMBX_PART_FWD], words, dest[QMBX_PART_FWD][(size_t)k_off], c, coef + 2 * t, t);
             Compiled a = compile_term(site + 4 * t, kind + 4 * t, fermi, true, below);
-            write_term(out, h.part[QMBX_PART_ADJ], h.n_words, k_off, a, coef + 2 * t, t);
+            write_term(out, h.part[QMBX_PART_ADJ], words, dest[QMBX_PART_ADJ][(size_t)k_off], a, coef + 2 * t, t);
             ++k_off;
         }
     }
+    std::memcpy(out, &h, sizeof(h));
     return QMBX_OK;
 }
 

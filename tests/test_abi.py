@@ -45,7 +45,9 @@ def test_version_and_no_error(lib):
 class Part(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("off_test", ctypes.c_uint64), ("off_apply", ctypes.c_uint64),
                 ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
-                ("off_norm", ctypes.c_uint64)]
+                ("off_norm", ctypes.c_uint64), ("off_groups", ctypes.c_uint64), ("off_single_ne", ctypes.c_uint64),
+                ("off_pair_ne", ctypes.c_uint64), ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
+                ("wide_groups", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Header(ctypes.Structure):
@@ -93,6 +95,34 @@ def from_key(key: list[int], nq: int) -> np.ndarray:
     return np.frombuffer(raw[:nq], dtype=np.uint8).copy()
 
 
+def check_groups(blob, h, which, part):
+    """Terms sit in the group of their two lowest required-occupied key positions, stable in input order."""
+    p = h.part[which]
+    w = h.n_words
+    groups = np.frombuffer(blob, dtype=np.int32, count=2 * p.n_groups, offset=p.off_groups).reshape(-1, 2)
+    single_ne = np.frombuffer(blob, dtype=np.uint64, count=w, offset=p.off_single_ne)
+    pair_ne = np.frombuffer(blob, dtype=np.uint64, count=64 * w * w, offset=p.off_pair_ne).reshape(64 * w, w)
+    test, _, _, orig = part
+    assert groups[0, 0] == 0 and groups[-1, 1] == p.n
+    assert np.all(groups[1:, 0] == groups[:-1, 1])
+    P = 64 * w
+    for g in np.nonzero(groups[:, 1] > groups[:, 0])[0]:
+        lo, hi = groups[g]
+        assert list(orig[lo:hi]) == sorted(orig[lo:hi])
+        for slot in range(lo, hi):
+            req = [64 * q + b for q in range(w) for b in range(64)
+                   if (int(test[slot, q, 0]) & int(test[slot, q, 1])) >> b & 1]
+            if len(req) >= 2:
+                a, b = req[0], req[1]
+                assert g == 1 + P + b * (b - 1) // 2 + a
+                assert int(pair_ne[a, b >> 6]) >> (b & 63) & 1
+            elif len(req) == 1:
+                assert g == 1 + req[0]
+                assert int(single_ne[req[0] >> 6]) >> (req[0] & 63) & 1
+            else:
+                assert g == 0
+
+
 def closed_form(test, apply, key):
     for q, word in enumerate(key):
         mask, val = int(test[q, 0]), int(test[q, 1])
@@ -117,11 +147,14 @@ def test_compiled_terms_reproduce_the_operator_walk(lib, case):
     adj = read_part(blob, h, 1)
     diag = read_part(blob, h, 2)
     assert fwd[0].shape[0] == adj[0].shape[0]
-    # every live term appears exactly once, in input order within each part
+    # every live term appears exactly once; the adjoint part holds the same terms as the forward part
     live = []
     for part in (fwd, diag):
         live.extend(part[3].tolist())
-        assert list(part[3]) == sorted(part[3])
+    assert len(live) == len(set(live))
+    assert sorted(fwd[3].tolist()) == sorted(adj[3].tolist())
+    for which, part in ((0, fwd), (1, adj), (2, diag)):
+        check_groups(blob, h, which, part)
     for t in range(site.shape[0]):
         ok_any = any(oracle.apply_term(site[t], kind[t], r, pc)[0] for r in rows[:40])
         if ok_any:
