@@ -109,28 +109,37 @@ struct GatherF64 : VisitorBase {
     const double2* val;      // one amplitude per unique looked-up key
     const double2* coef;     // coefficients of the walked part
     const double2* dcoef;    // coefficients of the diagonal part
-    double2* out;
-    const int32_t* out_first;  // forward: row of the first occurrence of each target
-    const int32_t* run_start;  // adjoint: sorted-position runs of each source key
-    const int32_t* run_perm;
+    const int32_t* unique;   // walk index -> first row of the walked key
+    double2* res;            // result per first row of the walked side
     struct Acc {
         double re, im, dre, dim;
     };
     __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.re = a.im = a.dre = a.dim = 0.0; }
-    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        int64_t pos = hash_find<W>(lookup, img);
-        if (pos < 0) return;
+    static constexpr bool kBatched = true;
+    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        const int64_t pos = hash_find<W>(lookup, img);
+        if (pos < 0) return false;
+        h = make_int2((int)slot | (parity << 31), (int)pos);
+        return true;
+    }
+    __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
+        const int slot = h.x & 0x7fffffff;
         double2 cf = __ldg(coef + slot);
-        double2 p = __ldg(val + pos);
+        double2 p = __ldg(val + h.y);
         double ci = CONJ ? -cf.y : cf.y;
         double re = cf.x * p.x - ci * p.y;
         double im = cf.x * p.y + ci * p.x;
-        if (parity) {
+        if (h.x < 0) {
             re = -re;
             im = -im;
         }
         a.re += re;
         a.im += im;
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
+        int2 h;
+        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         double2 cf = __ldg(dcoef + slot);
@@ -153,12 +162,7 @@ struct GatherF64 : VisitorBase {
                 a.im += a.dre * p.y + a.dim * p.x;
             }
         }
-        double2 r = make_double2(a.re, a.im);
-        if (!CONJ) {
-            out[out_first[u]] = r;
-        } else {
-            for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) out[run_perm[k]] = r;
-        }
+        res[__ldg(unique + u)] = make_double2(a.re, a.im);
     }
 };
 
@@ -169,11 +173,8 @@ struct GatherF32C : VisitorBase {
     const float4* coef32;
     const double2* dcoef;
     int include_diag;
-    double2* out64;
-    float2* out32;
-    const int32_t* out_first;
-    const int32_t* run_start;
-    const int32_t* run_perm;
+    const int32_t* unique;
+    double2* res;
     struct Acc {
         CompSum re, im;
         double dre, dim;
@@ -183,10 +184,20 @@ struct GatherF32C : VisitorBase {
         a.im.zero();
         a.dre = a.dim = 0.0;
     }
-    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        int64_t pos = hash_find<W>(lookup, img);
-        if (pos < 0) return;
-        comp_cmul_add<CONJ>(a.re, a.im, __ldg(coef32 + slot), __ldg(val + pos), parity);
+    static constexpr bool kBatched = true;
+    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        const int64_t pos = hash_find<W>(lookup, img);
+        if (pos < 0) return false;
+        h = make_int2((int)slot | (parity << 31), (int)pos);
+        return true;
+    }
+    __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
+        comp_cmul_add<CONJ>(a.re, a.im, __ldg(coef32 + (h.x & 0x7fffffff)), __ldg(val + h.y), h.x < 0 ? 1 : 0);
+    }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
+        int2 h;
+        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         double2 cf = __ldg(dcoef + slot);
@@ -210,17 +221,7 @@ struct GatherF32C : VisitorBase {
                 im += a.dre * (double)p.y + a.dim * (double)p.x;
             }
         }
-        if (!CONJ) {
-            int32_t r = out_first[u];
-            if (out64) out64[r] = make_double2(re, im);
-            if (out32) out32[r] = make_float2((float)re, (float)im);
-        } else {
-            for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) {
-                int32_t r = run_perm[k];
-                if (out64) out64[r] = make_double2(re, im);
-                if (out32) out32[r] = make_float2((float)re, (float)im);
-            }
-        }
+        res[__ldg(unique + u)] = make_double2(re, im);
     }
 };
 
@@ -253,7 +254,8 @@ struct DiagonalF64 : VisitorBase {
 template <int W, bool CONJ, bool F32>
 struct Scatter : VisitorBase {
     HashView lookup;        // output-side row set
-    const void* val;        // amplitude per unique walked key (double2, or float2 for F32)
+    const void* val;        // amplitude per first row of the walked side (double2, or float2 for F32)
+    const int32_t* unique;  // walk index -> first row of the walked key
     const double2* coef;    // walked part, FP64
     const float4* coef32;   // walked part, hi/lo FP32
     const double2* dcoef;   // diagonal part
@@ -263,7 +265,8 @@ struct Scatter : VisitorBase {
         double2 p;
         double dre, dim;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t row, const Key<W>&, int*) const {
+    __device__ __forceinline__ void init(Acc& a, int64_t u, const Key<W>&, int*) const {
+        const int64_t row = __ldg(unique + u);
         if (F32) {
             float2 q = __ldg(static_cast<const float2*>(val) + row);
             a.p = make_double2((double)q.x, (double)q.y);
@@ -272,9 +275,18 @@ struct Scatter : VisitorBase {
         }
         a.dre = a.dim = 0.0;
     }
-    __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        int64_t u = hash_find<W>(lookup, img);
-        if (u < 0) return;
+    static constexpr bool kBatched = true;
+    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        const int64_t u = hash_find<W>(lookup, img);
+        if (u < 0) return false;
+        h = make_int2((int)slot | (parity << 31), (int)u);
+        return true;
+    }
+    __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
+        const int64_t slot = h.x & 0x7fffffff;
+        const int64_t u = h.y;
+        const int parity = h.x < 0 ? 1 : 0;
         double re, im;
         if (F32) {
             float4 cf = __ldg(coef32 + slot);
@@ -302,6 +314,10 @@ struct Scatter : VisitorBase {
         atomicAdd(&acc[u].x, re);
         atomicAdd(&acc[u].y, im);
     }
+    __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
+        int2 h;
+        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
+    }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         double2 cf = __ldg(dcoef + slot);
         double ci = CONJ ? -cf.y : cf.y;
@@ -321,57 +337,37 @@ struct Scatter : VisitorBase {
     }
 };
 
-// Scatter results: forward writes the first occurrence of each output key,
-// adjoint every row of its run.
-__global__ void scatter_finalize_kernel(const double2* __restrict__ acc, const int* __restrict__ count,
-                                        const int32_t* __restrict__ first, const int32_t* __restrict__ run_start,
-                                        const int32_t* __restrict__ run_perm, double2* __restrict__ out64,
-                                        float2* __restrict__ out32) {
-    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= *count) return;
-    double2 r = acc[u];
-    if (first) {
-        if (out64) out64[first[u]] = r;
-        if (out32) out32[first[u]] = make_float2((float)r.x, (float)r.y);
-    } else {
-        for (int32_t k = run_start[u]; k < run_start[u + 1]; ++k) {
-            if (out64) out64[run_perm[k]] = r;
-            if (out32) out32[run_perm[k]] = make_float2((float)r.x, (float)r.y);
-        }
-    }
+// Write the user's output rows from the per-first-row results: the forward
+// map gives each key's value to its first row only (repeated rows get zero),
+// the adjoint gives it to every row holding the key.
+__global__ void apply_finalize_kernel(const double2* __restrict__ res, const int32_t* __restrict__ first, int64_t n,
+                                      int every_row, double2* __restrict__ out64, float2* __restrict__ out32) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t f = __ldg(first + i);
+    double2 r = make_double2(0.0, 0.0);
+    if (f >= 0 && (every_row || f == i)) r = res[f];
+    if (out64) out64[i] = r;
+    if (out32) out32[i] = make_float2((float)r.x, (float)r.y);
 }
 
 // ---------------------------------------------------------------------------
 // per-unique-key amplitudes
 // ---------------------------------------------------------------------------
 
-// Sum of the amplitudes of every row in each unique key's run, in sorted
-// (= original row) order.
+// Sum of the amplitudes of every row holding a key, stored at its first row
+// (one exact add per row without repeats).
 template <class T>
-__global__ void run_sum_kernel(const T* __restrict__ psi, const int32_t* __restrict__ perm,
-                               const int32_t* __restrict__ start, const int* __restrict__ count, T* __restrict__ out) {
-    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= *count) return;
-    int32_t a = start[u], b = start[u + 1];
-    double re = 0.0, im = 0.0;
-    for (int32_t k = a; k < b; ++k) {
-        T p = psi[perm[k]];
-        re += (double)p.x;
-        im += (double)p.y;
-    }
-    T r;
-    r.x = re;
-    r.y = im;
-    out[u] = r;
-}
-
-// Amplitude of the first occurrence of each unique key.
-template <class T>
-__global__ void first_value_kernel(const T* __restrict__ psi, const int32_t* __restrict__ first,
-                                   const int* __restrict__ count, T* __restrict__ out) {
-    int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= *count) return;
-    out[u] = psi[first[u]];
+__global__ void sum_repeats_kernel(const T* __restrict__ psi, const int32_t* __restrict__ first, int64_t n,
+                                   T* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t f = __ldg(first + i);
+    if (f < 0) return;
+    const T p = psi[i];
+    T* o = out + f;
+    atomicAdd(&o->x, p.x);
+    atomicAdd(&o->y, p.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -396,11 +392,12 @@ struct ApplyArgs {
     int include_diag;
 };
 
-// Launch one enumeration over `walk` rows: the grouped kernel (warp per row)
-// when the walked part is large, the tiled kernel (thread per row) otherwise.
+// Launch one enumeration over the unique rows of `walk`: the grouped kernel
+// (warp per row) when the walked part is large, the tiled kernel (thread per
+// row) otherwise.
 template <int W, class V>
-int launch_walk(const V& v, const RowSet& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
-    KeyRows<W> src{walk.keys};
+int launch_walk(const V& v, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
+    UniqueRows<W> src{walk.keys, walk.unique};
     if (part.n >= kGroupedMinTerms) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
     } else {
@@ -412,54 +409,52 @@ int launch_walk(const V& v, const RowSet& walk, const PartView& part, const Part
 
 // Forward maps amplitudes on configs_i (input side) to configs_j (output
 // side); the adjoint maps configs_j to configs_i.  Gather walks the output
-// side (daggered terms for the forward map), scatter walks the input side
-// (forward terms for the forward map) and adds into the output side with
-// atomics; the cheaper walk (fewer rows) is taken.
+// side's distinct rows (daggered terms for the forward map) and sums in
+// registers; scatter walks the input side's distinct rows (forward terms
+// for the forward map) and adds into the output side with FP64 atomics; the
+// walk over fewer rows is taken.  Both leave one result per distinct output
+// row, which apply_finalize_kernel spreads to the user's rows.
 template <int W>
 int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     const qmbx_table_header* h = header_of(a.table_host);
     const int nq = h->n_qubytes;
-    RowSet rs_i = take_rowset<W>(ws, a.n_i);
-    RowSet rs_j = a.same ? rs_i : take_rowset<W>(ws, a.n_j);
+    HashRows rs_i = take_hashrows<W>(ws, a.n_i);
+    HashRows rs_j = a.same ? rs_i : take_hashrows<W>(ws, a.n_j);
     const int64_t n_in = a.adjoint ? a.n_j : a.n_i;
     const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
-    void* uval = a.prec == Prec::F64 ? (void*)ws.take<double2>((uint64_t)(n_in > 0 ? n_in : 1))
-                                     : (void*)ws.take<float2>((uint64_t)(n_in > 0 ? n_in : 1));
-    double2* acc = ws.take<double2>((uint64_t)(n_out > 0 ? n_out : 1));
+    const size_t val_size = a.prec == Prec::F64 ? sizeof(double2) : sizeof(float2);
+    void* summed = ws.take<unsigned char>((uint64_t)(n_in > 0 ? n_in : 1) * val_size);
+    double2* res = ws.take<double2>((uint64_t)(n_out > 0 ? n_out : 1));
     if (ws.base == nullptr) return QMBX_OK;
     if (!ws.fits()) {
         return fail(QMBX_ERR_WORKSPACE, "workspace of %llu bytes is smaller than the %llu needed",
                     (unsigned long long)ws.cap, (unsigned long long)ws.used);
     }
     if (n_out == 0) return QMBX_OK;
-    if (a.out64) QMBX_CUDA_TRY(cudaMemsetAsync(a.out64, 0, (size_t)n_out * sizeof(double2), s));
-    if (a.out32) QMBX_CUDA_TRY(cudaMemsetAsync(a.out32, 0, (size_t)n_out * sizeof(float2), s));
     int st;
-    if ((st = build_rowset<W>(a.configs_i, nq, rs_i, s)) != QMBX_OK) return st;
-    if (!a.same && (st = build_rowset<W>(a.configs_j, nq, rs_j, s)) != QMBX_OK) return st;
-    if (n_in == 0) return QMBX_OK;
-
-    const RowSet& in_set = a.adjoint ? rs_j : rs_i;
-    const RowSet& out_set = a.adjoint ? rs_i : rs_j;
-    // per-unique-key amplitude of the input side: the forward map sums repeated
-    // source rows, the adjoint reads the first occurrence of each target row
-    const unsigned grid_in = grid_for(n_in, kThreads);
-    if (a.prec == Prec::F64) {
-        const double2* in = static_cast<const double2*>(a.in);
-        if (a.adjoint) {
-            QMBX_KERNEL(kGroupOther, s, first_value_kernel<double2><<<grid_in, kThreads, 0, s>>>(in, in_set.first, in_set.count, (double2*)uval));
-        } else {
-            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<double2><<<grid_in, kThreads, 0, s>>>(in, in_set.perm, in_set.start, in_set.count, (double2*)uval));
-        }
-    } else {
-        const float2* in = static_cast<const float2*>(a.in);
-        if (a.adjoint) {
-            QMBX_KERNEL(kGroupOther, s, first_value_kernel<float2><<<grid_in, kThreads, 0, s>>>(in, in_set.first, in_set.count, (float2*)uval));
-        } else {
-            QMBX_KERNEL(kGroupOther, s, run_sum_kernel<float2><<<grid_in, kThreads, 0, s>>>(in, in_set.perm, in_set.start, in_set.count, (float2*)uval));
-        }
+    if (n_in == 0) {
+        if (a.out64) QMBX_CUDA_TRY(cudaMemsetAsync(a.out64, 0, (size_t)n_out * sizeof(double2), s));
+        if (a.out32) QMBX_CUDA_TRY(cudaMemsetAsync(a.out32, 0, (size_t)n_out * sizeof(float2), s));
+        return QMBX_OK;
     }
-    QMBX_LAUNCH_CHECK("amplitude gather");
+    if ((st = build_hashrows<W>(a.configs_i, nq, rs_i, s)) != QMBX_OK) return st;
+    if (!a.same && (st = build_hashrows<W>(a.configs_j, nq, rs_j, s)) != QMBX_OK) return st;
+    const HashRows& in_set = a.adjoint ? rs_j : rs_i;
+    const HashRows& out_set = a.adjoint ? rs_i : rs_j;
+
+    // amplitude per first row of the input side: the forward map sums
+    // repeated source rows; the adjoint reads the first occurrence as given
+    const void* val = a.in;
+    if (!a.adjoint) {
+        QMBX_CUDA_TRY(cudaMemsetAsync(summed, 0, (size_t)n_in * val_size, s));
+        if (a.prec == Prec::F64) {
+            QMBX_KERNEL(kGroupOther, s, sum_repeats_kernel<double2><<<grid_for(n_in, kThreads), kThreads, 0, s>>>(static_cast<const double2*>(a.in), in_set.first, n_in, static_cast<double2*>(summed)));
+        } else {
+            QMBX_KERNEL(kGroupOther, s, sum_repeats_kernel<float2><<<grid_for(n_in, kThreads), kThreads, 0, s>>>(static_cast<const float2*>(a.in), in_set.first, n_in, static_cast<float2*>(summed)));
+        }
+        QMBX_LAUNCH_CHECK("sum_repeats_kernel");
+        val = summed;
+    }
 
     PartView fwd = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     PartView adj = part_view(a.table_host, a.table_dev, QMBX_PART_ADJ);
@@ -471,50 +466,52 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         // walk the input side: forward terms for the forward map, daggered
         // terms (conjugated) for the adjoint
         const PartView& part = a.adjoint ? adj : fwd;
-        QMBX_CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)n_out * sizeof(double2), s));
+        QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
+        const HashView look = out_set.hash();
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
-                Scatter<W, true, false> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, 1, acc};
-                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+                Scatter<W, true, false> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, 1, res};
+                st = launch_walk<W>(v, in_set, part, diag, s);
             } else {
-                Scatter<W, false, false> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, 1, acc};
-                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+                Scatter<W, false, false> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, 1, res};
+                st = launch_walk<W>(v, in_set, part, diag, s);
             }
         } else {
             if (a.adjoint) {
-                Scatter<W, true, true> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, include_diag, acc};
-                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+                Scatter<W, true, true> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                st = launch_walk<W>(v, in_set, part, diag, s);
             } else {
-                Scatter<W, false, true> v{{}, out_set.hash(), uval, part.coef, part.coef32, diag.coef, include_diag, acc};
-                if ((st = launch_walk<W>(v, in_set, part, diag, s)) != QMBX_OK) return st;
+                Scatter<W, false, true> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                st = launch_walk<W>(v, in_set, part, diag, s);
             }
         }
-        QMBX_KERNEL(kGroupOther, s, scatter_finalize_kernel<<<grid_for(n_out, kThreads), kThreads, 0, s>>>(
-            acc, out_set.count, a.adjoint ? nullptr : out_set.first, out_set.start, out_set.perm, a.out64, a.out32));
-        QMBX_LAUNCH_CHECK("scatter_finalize_kernel");
-        return QMBX_OK;
-    }
-    // gather: walk the output side with daggered terms for the forward map,
-    // forward terms (conjugated) for the adjoint
-    const PartView& part = a.adjoint ? fwd : adj;
-    if (a.prec == Prec::F64) {
-        if (!a.adjoint) {
-            GatherF64<W, false> v{{}, in_set.hash(), (const double2*)uval, part.coef, diag.coef, a.out64, out_set.first,
-                                  nullptr, nullptr};
-            return launch_walk<W>(v, out_set, part, diag, s);
+    } else {
+        // gather: walk the output side with daggered terms for the forward
+        // map, forward terms (conjugated) for the adjoint
+        const PartView& part = a.adjoint ? fwd : adj;
+        const HashView look = in_set.hash();
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
+                st = launch_walk<W>(v, out_set, part, diag, s);
+            } else {
+                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
+                st = launch_walk<W>(v, out_set, part, diag, s);
+            }
+        } else {
+            if (a.adjoint) {
+                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
+                st = launch_walk<W>(v, out_set, part, diag, s);
+            } else {
+                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
+                st = launch_walk<W>(v, out_set, part, diag, s);
+            }
         }
-        GatherF64<W, true> v{{}, in_set.hash(), (const double2*)uval, part.coef, diag.coef, a.out64, nullptr,
-                             out_set.start, out_set.perm};
-        return launch_walk<W>(v, out_set, part, diag, s);
     }
-    if (!a.adjoint) {
-        GatherF32C<W, false> v{{}, in_set.hash(), (const float2*)uval, part.coef32, diag.coef, a.include_diag, a.out64,
-                               a.out32, out_set.first, nullptr, nullptr};
-        return launch_walk<W>(v, out_set, part, diag, s);
-    }
-    GatherF32C<W, true> v{{}, in_set.hash(), (const float2*)uval, part.coef32, diag.coef, a.include_diag, a.out64,
-                          a.out32, nullptr, out_set.start, out_set.perm};
-    return launch_walk<W>(v, out_set, part, diag, s);
+    if (st != QMBX_OK) return st;
+    QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_out, kThreads), kThreads, 0, s>>>(res, out_set.first, n_out, a.adjoint ? 1 : 0, a.out64, a.out32));
+    QMBX_LAUNCH_CHECK("apply_finalize_kernel");
+    return QMBX_OK;
 }
 
 int dispatch_apply(const ApplyArgs& a, Arena& ws, cudaStream_t s) {

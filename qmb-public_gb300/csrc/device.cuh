@@ -276,6 +276,9 @@ __device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, co
 // no per-block set-up or flush.
 struct VisitorBase {
     static constexpr int kShared = 0;
+    static constexpr bool kBatched = false;
+    template <class Acc>
+    __device__ __forceinline__ void apply_hit(Acc&, int2) const {}
     __device__ __forceinline__ void block_init(int*) const {}
     __device__ __forceinline__ void block_flush(int*) const {}
 };
@@ -357,14 +360,51 @@ constexpr int kWarpsPerBlock = kThreads / 32;
 // Parts with at least this many terms are walked by grouped_kernel.
 constexpr int64_t kGroupedMinTerms = 2048;
 
+// Hits of batched visitors wait in a per-warp shared queue until 32 have
+// gathered, then every lane processes one: the floating-point work of a hit
+// (FP64 on GB300 issues at a small fraction of the FP32 rate) then runs with
+// all lanes active instead of once per divergent warp iteration.
+struct HitQueue {
+    int2* q;    // 64 entries: (slot | parity << 31, looked-up row)
+    int count;  // warp-uniform
+};
+
+template <class V>
+__device__ __forceinline__ void queue_drain(const V& v, typename V::Acc& acc, HitQueue& hq, int lane, bool all) {
+    if (all) {
+        if (lane < hq.count) v.apply_hit(acc, hq.q[lane]);
+        __syncwarp();
+        hq.count = 0;
+        return;
+    }
+    v.apply_hit(acc, hq.q[lane]);
+    __syncwarp();
+    if (lane < hq.count - 32) hq.q[lane] = hq.q[32 + lane];
+    __syncwarp();
+    hq.count -= 32;
+}
+
+template <class V>
+__device__ __forceinline__ void queue_push(const V& v, typename V::Acc& acc, HitQueue& hq, int lane, bool hit,
+                                           int2 h) {
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m == 0) return;
+    if (hit) hq.q[hq.count + __popc(m & ((1u << lane) - 1u))] = h;
+    hq.count += __popc(m);
+    __syncwarp();
+    if (hq.count >= 32) queue_drain(v, acc, hq, lane, false);
+}
+
+// Test term t against c; on success either visit it directly or, for a
+// batched visitor, probe it and report a hit to queue.
 template <int W, bool DIAG, class V>
-__device__ __forceinline__ void visit_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                           int64_t t) {
+__device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
+                                          int64_t t, int2& h) {
     const uint64_t* test = pv.test + t * 2 * W;
     uint64_t bad = 0;
 #pragma unroll
     for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ __ldg(test + 2 * q + 1)) & __ldg(test + 2 * q);
-    if (bad) return;
+    if (bad) return false;
     const uint64_t* ap = pv.apply + t * 2 * W;
     Key<W> img;
     int par = 0;
@@ -375,39 +415,52 @@ __device__ __forceinline__ void visit_term(const V& v, typename V::Acc& acc, con
     }
     if (DIAG) {
         v.visit_diag(acc, c, par & 1, t);
+        return false;
+    } else if constexpr (V::kBatched) {
+        return v.probe(acc, c, img, par & 1, t, h);
     } else {
         v.visit(acc, c, img, par & 1, t);
+        return false;
     }
 }
 
-// Walk one group: lanes over its terms.
+// Walk one group: lanes over its terms (warp-uniform bounds, so hits can be queued).
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& acc, const Key<W>& c,
-                                                 const PartView& pv, int64_t g, int lane) {
+                                                 const PartView& pv, int64_t g, int lane, HitQueue& hq) {
     const int2 se = __ldg(pv.groups + g);
-    for (int64_t t = se.x + lane; t < se.y; t += 32) visit_term<W, DIAG>(v, acc, c, pv, t);
+    for (int64_t base = se.x; base < se.y; base += 32) {
+        const int64_t t = base + lane;
+        int2 h = make_int2(0, 0);
+        bool hit = false;
+        if (t < se.y) hit = test_term<W, DIAG>(v, acc, c, pv, t, h);
+        if constexpr (V::kBatched && !DIAG) queue_push(v, acc, hq, lane, hit, h);
+    }
 }
 
-// Walk one group entirely in this lane.
+// Walk one group entirely in this lane (hits processed at once).
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& acc, const Key<W>& c,
                                                   const PartView& pv, int64_t g) {
     const int2 se = __ldg(pv.groups + g);
-    for (int64_t t = se.x; t < se.y; ++t) visit_term<W, DIAG>(v, acc, c, pv, t);
+    for (int64_t t = se.x; t < se.y; ++t) {
+        int2 h;
+        if (test_term<W, DIAG>(v, acc, c, pv, t, h)) v.apply_hit(acc, h);
+    }
 }
 
 // Visit the groups named by the set bits of a 64-bit mask (key positions
-// 64 * word + bit), as single groups (second < 0) or pair groups with first.
+// 64 * word + bit), as single groups (first < 0) or pair groups with first.
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                          uint64_t bits, int word, int first, int lane) {
+                                          uint64_t bits, int word, int first, int lane, HitQueue& hq) {
     if (pv.wide) {
         while (bits) {
             const int b = __ffsll((long long)bits) - 1;
             bits &= bits - 1;
             const int kp = 64 * word + b;
             const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
-            walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane);
+            walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
         }
     } else {
 #pragma unroll
@@ -419,16 +472,17 @@ __device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, cons
                 walk_group_serial<W, DIAG>(v, acc, c, pv, g);
             }
         }
+        __syncwarp();
     }
 }
 
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                          int lane) {
+                                          int lane, HitQueue& hq) {
     if (pv.n == 0) return;
-    walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane);
+    walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane, hq);
 #pragma unroll
-    for (int q = 0; q < W; ++q) walk_mask<W, DIAG>(v, acc, c, pv, c.w[q] & __ldg(pv.single_ne + q), q, -1, lane);
+    for (int q = 0; q < W; ++q) walk_mask<W, DIAG>(v, acc, c, pv, c.w[q] & __ldg(pv.single_ne + q), q, -1, lane, hq);
 #pragma unroll
     for (int q = 0; q < W; ++q) {
         uint64_t occ = c.w[q];
@@ -440,7 +494,7 @@ __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, cons
 #pragma unroll
             for (int r = 0; r < W; ++r) {
                 if (r < q) continue;  // partners sit at higher key positions
-                walk_mask<W, DIAG>(v, acc, c, pv, c.w[r] & __ldg(pn + r), r, kp, lane);
+                walk_mask<W, DIAG>(v, acc, c, pv, c.w[r] & __ldg(pn + r), r, kp, lane, hq);
             }
         }
     }
@@ -450,17 +504,21 @@ template <int W, class V, class Src>
 __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const int* __restrict__ n_rows,
                                                            int64_t n_max, PartView off, PartView diag) {
     __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
+    __shared__ int2 hitq[kWarpsPerBlock][64];
     v.block_init(sh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
     const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlock;
-    for (int64_t row = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); row < n; row += stride) {
+    for (int64_t row = (int64_t)blockIdx.x * kWarpsPerBlock + warp; row < n; row += stride) {
         const Key<W> c = src.get(row);
         typename V::Acc acc;
         v.init(acc, row, c, sh);
-        walk_part<W, false>(v, acc, c, off, lane);
-        walk_part<W, true>(v, acc, c, diag, lane);
+        HitQueue hq{hitq[warp], 0};
+        walk_part<W, false>(v, acc, c, off, lane, hq);
+        if constexpr (V::kBatched) queue_drain(v, acc, hq, lane, true);
+        walk_part<W, true>(v, acc, c, diag, lane, hq);
         v.reduce(acc);
         if (lane == 0) v.finish(acc, row, c);
     }
@@ -532,6 +590,40 @@ RowSet take_rowset(Arena& ws, int64_t n);
 
 template <int W>
 int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s);
+
+// A de-duplicated row set without sorting: every row's key is inserted in an
+// open-addressing hash set whose entries name the first (lowest) row holding
+// that key.  first[i] is that row for every row i; unique[0 .. *count) lists
+// the first rows in row order.  Lookups (hash()) return first rows, so
+// per-key data is stored at the first row's index.
+struct HashRows {
+    uint64_t* keys;     // n x W, row order
+    uint64_t* slots;
+    uint64_t slot_mask;
+    int32_t* first;     // n
+    int32_t* unique;    // n (first *count valid)
+    int32_t* head;      // n: 1 where first[i] == i
+    int32_t* pos;       // n
+    int* count;
+    int32_t* scan;      // scan scratch
+    int64_t n;
+    HashView hash() const { return HashView{slots, keys, slot_mask}; }
+};
+
+template <int W>
+HashRows take_hashrows(Arena& ws, int64_t n);
+
+template <int W>
+int build_hashrows(const uint8_t* rows, int n_qubytes, HashRows& out, cudaStream_t s);
+
+// Rows of a HashRows set visited by the enumeration kernels: walk index u
+// is the u-th unique row.
+template <int W>
+struct UniqueRows {
+    const uint64_t* keys;
+    const int32_t* unique;
+    __device__ __forceinline__ Key<W> get(int64_t u) const { return load_key<W>(keys, __ldg(unique + u)); }
+};
 
 // Exclusive prefix sum of n int32 values (in == out allowed); the total goes
 // to *total when non-NULL.  scratch holds scan_scratch(n) int32 values.

@@ -420,6 +420,94 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     return QMBX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// hash-based de-duplicated row sets
+// ---------------------------------------------------------------------------
+
+// Insert every row; a key already present keeps the lowest row (64-bit
+// atomicMin over entries that share the fingerprint, i.e. the same key).
+template <int W>
+__global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint64_t* __restrict__ slots,
+                                       uint64_t mask) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const Key<W> k = load_key<W>(keys, r);
+    const uint64_t hv = key_hash<W>(k);
+    const uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)r;
+    uint64_t i = hv & mask;
+    unsigned long long* sl = reinterpret_cast<unsigned long long*>(slots);
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+        unsigned long long cur = sl[i];
+        if (cur == (unsigned long long)kEmptySlot) {
+            cur = atomicCAS(sl + i, (unsigned long long)kEmptySlot, (unsigned long long)entry);
+            if (cur == (unsigned long long)kEmptySlot) return;
+        }
+        if ((uint32_t)(cur >> 32) == (uint32_t)(entry >> 32) && key_eq<W>(load_key<W>(keys, (int64_t)(uint32_t)cur), k)) {
+            atomicMin(sl + i, (unsigned long long)entry);
+            return;
+        }
+        i = (i + 1) & mask;
+    }
+}
+
+// first[r] = lowest row with row r's key; head[r] = (first[r] == r).
+template <int W>
+__global__ void hashrows_resolve_kernel(const uint64_t* __restrict__ keys, int64_t n, HashView h,
+                                        int32_t* __restrict__ first, int32_t* __restrict__ head) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int64_t f = hash_find<W>(h, load_key<W>(keys, r));
+    first[r] = (int32_t)f;
+    head[r] = f == r ? 1 : 0;
+}
+
+__global__ void hashrows_compact_kernel(const int32_t* __restrict__ head, const int32_t* __restrict__ pos, int64_t n,
+                                        int32_t* __restrict__ unique, int* __restrict__ count) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    if (head[r]) unique[pos[r]] = (int32_t)r;
+    if (r == n - 1) *count = pos[r] + head[r];
+}
+
+template <int W>
+HashRows take_hashrows(Arena& ws, int64_t n) {
+    HashRows out;
+    uint64_t cap = (uint64_t)(n > 0 ? n : 1);
+    out.n = n;
+    out.keys = ws.take<uint64_t>(cap * W);
+    uint64_t slots = 64;
+    while (slots < 2 * cap) slots <<= 1;
+    out.slots = ws.take<uint64_t>(slots);
+    out.slot_mask = slots - 1;
+    out.first = ws.take<int32_t>(cap);
+    out.unique = ws.take<int32_t>(cap);
+    out.head = ws.take<int32_t>(cap);
+    out.pos = ws.take<int32_t>(cap);
+    out.count = ws.take<int>(1);
+    out.scan = ws.take<int32_t>((uint64_t)scan_scratch((int64_t)cap));
+    return out;
+}
+
+template <int W>
+int build_hashrows(const uint8_t* rows, int nq, HashRows& out, cudaStream_t s) {
+    const int64_t n = out.n;
+    QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
+    if (n == 0) {
+        QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
+        QMBX_LAUNCH_CHECK("set_int_kernel");
+        return QMBX_OK;
+    }
+    int st;
+    if ((st = pack_rows<W>(rows, n, nq, out.keys, s)) != QMBX_OK) return st;
+    const unsigned grid = grid_for(n, kThreads);
+    QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.slots, out.slot_mask));
+    QMBX_KERNEL(kGroupKeys, s, hashrows_resolve_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.hash(), out.first, out.head));
+    if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.scan, s)) != QMBX_OK) return st;
+    QMBX_KERNEL(kGroupKeys, s, hashrows_compact_kernel<<<grid, kThreads, 0, s>>>(out.head, out.pos, n, out.unique, out.count));
+    QMBX_LAUNCH_CHECK("build_hashrows");
+    return QMBX_OK;
+}
+
 #define QMBX_INSTANTIATE_KEYS(W)                                                                                \
     template int pack_rows<W>(const uint8_t*, int64_t, int, uint64_t*, cudaStream_t);                           \
     template int unpack_rows<W>(const uint64_t*, const int*, int64_t, int, uint8_t*, cudaStream_t);             \
@@ -427,7 +515,9 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     template int sort_pairs<W>(const uint64_t*, const int32_t*, uint64_t*, int32_t*, int64_t, int,              \
                                const SortScratch&, cudaStream_t);                                               \
     template RowSet take_rowset<W>(Arena&, int64_t);                                                            \
-    template int build_rowset<W>(const uint8_t*, int, RowSet&, cudaStream_t);
+    template int build_rowset<W>(const uint8_t*, int, RowSet&, cudaStream_t);                                   \
+    template HashRows take_hashrows<W>(Arena&, int64_t);                                                        \
+    template int build_hashrows<W>(const uint8_t*, int, HashRows&, cudaStream_t);
 
 QMBX_INSTANTIATE_KEYS(1)
 QMBX_INSTANTIATE_KEYS(2)

@@ -172,7 +172,7 @@ struct FindArgs {
 // final row set of up to k rows), then the emission area of cap records.
 template <int W>
 struct FindLayout {
-    RowSet excl;
+    HashRows excl;
     uint64_t* keys_i;
     unsigned long long* hist;
     unsigned long long* n_emit;
@@ -196,7 +196,7 @@ uint64_t record_bytes() {
 template <int W>
 FindLayout<W> take_find(Arena& ws, int64_t n_i, int64_t k, int64_t n_ex, int64_t cap) {
     FindLayout<W> L;
-    L.excl = take_rowset<W>(ws, n_ex);
+    L.excl = take_hashrows<W>(ws, n_ex);
     L.keys_i = ws.take<uint64_t>((uint64_t)(n_i > 0 ? n_i : 1) * W);
     L.hist = ws.take<unsigned long long>(kBuckets + 1);
     L.n_emit = L.hist + kBuckets;
@@ -241,7 +241,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     *a.n_out = 0;
     if (k == 0 || a.n_i == 0) return QMBX_OK;
     int st;
-    if ((st = build_rowset<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
+    if ((st = build_hashrows<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
     if ((st = pack_rows<W>(a.configs_i, a.n_i, nq, L.keys_i, s)) != QMBX_OK) return st;
     QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
     QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
@@ -395,14 +395,14 @@ struct SingleVisitor : VisitorBase {
 
 template <int W>
 struct SingleLayout {
-    RowSet set;
+    HashRows set;
     double* kf;
 };
 
 template <int W>
 SingleLayout<W> take_single(Arena& ws, int64_t n, int64_t n_off) {
     SingleLayout<W> L;
-    L.set = take_rowset<W>(ws, n);
+    L.set = take_hashrows<W>(ws, n);
     L.kf = ws.take<double>((uint64_t)(n_off > 0 ? n_off : 1));
     return L;
 }
@@ -417,7 +417,7 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     if (!ws.fits()) return fail(QMBX_ERR_WORKSPACE, "single_relative needs %llu bytes of workspace", (unsigned long long)ws.used);
     if (n == 0) return QMBX_OK;
     int st;
-    if ((st = build_rowset<W>(configs, h->n_qubytes, L.set, s)) != QMBX_OK) return st;
+    if ((st = build_hashrows<W>(configs, h->n_qubytes, L.set, s)) != QMBX_OK) return st;
     if (off.n > 0) {
         QMBX_KERNEL(kGroupOther, s, es_factor_kernel<<<grid_for(off.n, kThreads), kThreads, 0, s>>>(off.coef, off.orig, off.n, seed, L.kf));
         QMBX_LAUNCH_CHECK("es_factor_kernel");
@@ -425,7 +425,7 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     PartView none = off;
     none.n = 0;
     SingleVisitor<W> v{{}, L.set.hash(), L.kf, off.orig, out, h->n_qubytes};
-    KeyRows<W> src{L.set.packed};
+    KeyRows<W> src{L.set.keys};
     if (off.n >= kGroupedMinTerms) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
     } else {
