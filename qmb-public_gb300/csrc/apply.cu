@@ -116,12 +116,16 @@ struct GatherF64 : VisitorBase {
     };
     __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.re = a.im = a.dre = a.dim = 0.0; }
     static constexpr bool kBatched = true;
-    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
-                                          int2& h) const {
-        const int64_t pos = hash_find<W>(lookup, img);
+    static constexpr bool kProbe = true;
+    __device__ __forceinline__ bool take(Acc&, const Key<W>&, const Key<W>&, int parity, int64_t slot, int64_t pos,
+                                         int2& h) const {
         if (pos < 0) return false;
         h = make_int2((int)slot | (parity << 31), (int)pos);
         return true;
+    }
+    __device__ __forceinline__ bool probe(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        return take(a, c, img, parity, slot, hash_find<W>(lookup, img), h);
     }
     __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
         const int slot = h.x & 0x7fffffff;
@@ -185,12 +189,16 @@ struct GatherF32C : VisitorBase {
         a.dre = a.dim = 0.0;
     }
     static constexpr bool kBatched = true;
-    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
-                                          int2& h) const {
-        const int64_t pos = hash_find<W>(lookup, img);
+    static constexpr bool kProbe = true;
+    __device__ __forceinline__ bool take(Acc&, const Key<W>&, const Key<W>&, int parity, int64_t slot, int64_t pos,
+                                         int2& h) const {
         if (pos < 0) return false;
         h = make_int2((int)slot | (parity << 31), (int)pos);
         return true;
+    }
+    __device__ __forceinline__ bool probe(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        return take(a, c, img, parity, slot, hash_find<W>(lookup, img), h);
     }
     __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
         comp_cmul_add<CONJ>(a.re, a.im, __ldg(coef32 + (h.x & 0x7fffffff)), __ldg(val + h.y), h.x < 0 ? 1 : 0);
@@ -276,12 +284,16 @@ struct Scatter : VisitorBase {
         a.dre = a.dim = 0.0;
     }
     static constexpr bool kBatched = true;
-    __device__ __forceinline__ bool probe(Acc&, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
-                                          int2& h) const {
-        const int64_t u = hash_find<W>(lookup, img);
+    static constexpr bool kProbe = true;
+    __device__ __forceinline__ bool take(Acc&, const Key<W>&, const Key<W>&, int parity, int64_t slot, int64_t u,
+                                         int2& h) const {
         if (u < 0) return false;
         h = make_int2((int)slot | (parity << 31), (int)u);
         return true;
+    }
+    __device__ __forceinline__ bool probe(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot,
+                                          int2& h) const {
+        return take(a, c, img, parity, slot, hash_find<W>(lookup, img), h);
     }
     __device__ __forceinline__ void apply_hit(Acc& a, int2 h) const {
         const int64_t slot = h.x & 0x7fffffff;

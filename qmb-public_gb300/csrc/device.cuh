@@ -138,8 +138,7 @@ __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& ke
 // ---------------------------------------------------------------------------
 
 struct PartView {
-    const uint64_t* test;   // [n][2W] mask, val
-    const uint64_t* apply;  // [n][2W] flip, par
+    const uint64_t* term;   // [n][W][4] mask, val, flip, par
     const double2* coef;
     const float4* coef32;
     const int32_t* orig;
@@ -156,8 +155,7 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
     const qmbx_table_part& p = h->part[which];
     const char* base = static_cast<const char*>(table_dev);
     PartView v;
-    v.test = reinterpret_cast<const uint64_t*>(base + p.off_test);
-    v.apply = reinterpret_cast<const uint64_t*>(base + p.off_apply);
+    v.term = reinterpret_cast<const uint64_t*>(base + p.off_term);
     v.coef = reinterpret_cast<const double2*>(base + p.off_coef);
     v.coef32 = reinterpret_cast<const float4*>(base + p.off_coef32);
     v.orig = reinterpret_cast<const int32_t*>(base + p.off_orig);
@@ -182,30 +180,23 @@ constexpr int kTermTile = 128;
 
 template <int W>
 struct TermTile {
-    uint64_t m[kTermTile][4 * W];  // mask, val (2W) then flip, par (2W)
+    uint64_t m[kTermTile][4 * W];  // per word: mask, val, flip, par
 };
 
 template <int W>
 __device__ __forceinline__ void stage_tile(TermTile<W>& tile, const PartView& part, int64_t t0, int count) {
     // 4W words per term, copied as 16-byte pairs
-    const int pairs_per_term = 2 * W;
-    const int total = count * pairs_per_term;
-    for (int k = threadIdx.x; k < total; k += blockDim.x) {
-        int term = k / pairs_per_term;
-        int pr = k - term * pairs_per_term;
-        const uint64_t* src = pr < W ? part.test + (t0 + term) * 2 * W + 2 * pr
-                                     : part.apply + (t0 + term) * 2 * W + 2 * (pr - W);
-        ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(src));
-        tile.m[term][2 * pr] = v.x;
-        tile.m[term][2 * pr + 1] = v.y;
-    }
+    const int total = count * 2 * W;
+    const ulonglong2* src = reinterpret_cast<const ulonglong2*>(part.term + t0 * 4 * W);
+    ulonglong2* dst = reinterpret_cast<ulonglong2*>(&tile.m[0][0]);
+    for (int k = threadIdx.x; k < total; k += blockDim.x) dst[k] = __ldg(src + k);
 }
 
 template <int W>
 __device__ __forceinline__ bool term_applies(const uint64_t* t, const Key<W>& c) {
     uint64_t bad = 0;
 #pragma unroll
-    for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ t[2 * q + 1]) & t[2 * q];
+    for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ t[4 * q + 1]) & t[4 * q];
     return bad == 0;
 }
 
@@ -214,8 +205,8 @@ __device__ __forceinline__ int term_image(const uint64_t* t, const Key<W>& c, Ke
     int par = 0;
 #pragma unroll
     for (int q = 0; q < W; ++q) {
-        img.w[q] = c.w[q] ^ t[2 * W + 2 * q];
-        par += __popcll(c.w[q] & t[2 * W + 2 * q + 1]);
+        img.w[q] = c.w[q] ^ t[4 * q + 2];
+        par += __popcll(c.w[q] & t[4 * q + 3]);
     }
     return par & 1;
 }
@@ -276,7 +267,8 @@ __device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, co
 // no per-block set-up or flush.
 struct VisitorBase {
     static constexpr int kShared = 0;
-    static constexpr bool kBatched = false;
+    static constexpr bool kBatched = false;  // hits are queued and processed by apply_hit with full lanes
+    static constexpr bool kProbe = false;    // has `HashView lookup` and take(): lookups are pipelined
     template <class Acc>
     __device__ __forceinline__ void apply_hit(Acc&, int2) const {}
     __device__ __forceinline__ void block_init(int*) const {}
@@ -360,6 +352,40 @@ constexpr int kWarpsPerBlock = kThreads / 32;
 // Parts with at least this many terms are walked by grouped_kernel.
 constexpr int64_t kGroupedMinTerms = 2048;
 
+// One term record in registers (loaded with 16-byte vector loads).
+template <int W>
+struct TermRec {
+    uint64_t m[4 * W];
+    __device__ __forceinline__ bool applies(const Key<W>& c) const {
+        uint64_t bad = 0;
+#pragma unroll
+        for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ m[4 * q + 1]) & m[4 * q];
+        return bad == 0;
+    }
+    __device__ __forceinline__ int image(const Key<W>& c, Key<W>& img) const {
+        int par = 0;
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            img.w[q] = c.w[q] ^ m[4 * q + 2];
+            par += __popcll(c.w[q] & m[4 * q + 3]);
+        }
+        return par & 1;
+    }
+};
+
+template <int W>
+__device__ __forceinline__ TermRec<W> load_term(const PartView& pv, int64_t t) {
+    TermRec<W> r;
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(pv.term + t * 4 * W);
+#pragma unroll
+    for (int k = 0; k < 2 * W; ++k) {
+        ulonglong2 v = __ldg(p + k);
+        r.m[2 * k] = v.x;
+        r.m[2 * k + 1] = v.y;
+    }
+    return r;
+}
+
 // Hits of batched visitors wait in a per-warp shared queue until 32 have
 // gathered, then every lane processes one: the floating-point work of a hit
 // (FP64 on GB300 issues at a small fraction of the FP32 rate) then runs with
@@ -400,26 +426,17 @@ __device__ __forceinline__ void queue_push(const V& v, typename V::Acc& acc, Hit
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
                                           int64_t t, int2& h) {
-    const uint64_t* test = pv.test + t * 2 * W;
-    uint64_t bad = 0;
-#pragma unroll
-    for (int q = 0; q < W; ++q) bad |= (c.w[q] ^ __ldg(test + 2 * q + 1)) & __ldg(test + 2 * q);
-    if (bad) return false;
-    const uint64_t* ap = pv.apply + t * 2 * W;
+    TermRec<W> r = load_term<W>(pv, t);
+    if (!r.applies(c)) return false;
     Key<W> img;
-    int par = 0;
-#pragma unroll
-    for (int q = 0; q < W; ++q) {
-        img.w[q] = c.w[q] ^ __ldg(ap + 2 * q);
-        par += __popcll(c.w[q] & __ldg(ap + 2 * q + 1));
-    }
+    const int par = r.image(c, img);
     if (DIAG) {
-        v.visit_diag(acc, c, par & 1, t);
+        v.visit_diag(acc, c, par, t);
         return false;
     } else if constexpr (V::kBatched) {
-        return v.probe(acc, c, img, par & 1, t, h);
+        return v.probe(acc, c, img, par, t, h);
     } else {
-        v.visit(acc, c, img, par & 1, t);
+        v.visit(acc, c, img, par, t);
         return false;
     }
 }
@@ -435,6 +452,73 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
         bool hit = false;
         if (t < se.y) hit = test_term<W, DIAG>(v, acc, c, pv, t, h);
         if constexpr (V::kBatched && !DIAG) queue_push(v, acc, hq, lane, hit, h);
+    }
+}
+
+// hash_find split in two: the first slot is loaded by the caller (so that
+// several lookups can be in flight), the rest of the probe runs here.
+template <int W>
+__device__ __forceinline__ int64_t hash_resolve(const HashView& h, const Key<W>& key, uint64_t hv,
+                                                uint64_t first_slot) {
+    const uint32_t fp = (uint32_t)(hv >> 32);
+    uint64_t i = hv & h.mask;
+    uint64_t s = first_slot;
+    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
+        if (s == kEmptySlot) return -1;
+        if ((uint32_t)(s >> 32) == fp) {
+            const int64_t idx = (int64_t)(uint32_t)s;
+            if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
+        }
+        i = (i + 1) & h.mask;
+        s = __ldg(h.slots + i);
+    }
+    return -1;
+}
+
+// Walk one group with lanes over terms, kPipe terms per lane per step: the
+// term records of all kPipe are loaded, tested and hashed, then their first
+// hash slots are loaded together, so each lane keeps several independent
+// L2 requests in flight; v.take() sees each applicable term with the
+// lookup's answer.
+constexpr int kPipe = 4;
+
+template <int W, class V>
+__device__ __forceinline__ void walk_group_pipelined(const V& v, typename V::Acc& acc, const Key<W>& c,
+                                                     const PartView& pv, int64_t g, int lane, HitQueue& hq) {
+    const int2 se = __ldg(pv.groups + g);
+    for (int64_t base = se.x; base < se.y; base += 32 * kPipe) {
+        bool app[kPipe];
+        Key<W> img[kPipe];
+        int par[kPipe];
+        uint64_t hv[kPipe], s0[kPipe];
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) {
+            const int64_t t = base + 32 * k + lane;
+            app[k] = false;
+            par[k] = 0;
+            if (t < se.y) {
+                const TermRec<W> r = load_term<W>(pv, t);
+                app[k] = r.applies(c);
+                par[k] = r.image(c, img[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) {
+            if (app[k]) {
+                hv[k] = key_hash<W>(img[k]);
+                s0[k] = __ldg(v.lookup.slots + (hv[k] & v.lookup.mask));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) {
+            int2 h = make_int2(0, 0);
+            bool hit = false;
+            if (app[k]) {
+                const int64_t pos = hash_resolve<W>(v.lookup, img[k], hv[k], s0[k]);
+                hit = v.take(acc, c, img[k], par[k], base + 32 * k + lane, pos, h);
+            }
+            if constexpr (V::kBatched) queue_push(v, acc, hq, lane, hit, h);
+        }
     }
 }
 
@@ -460,7 +544,11 @@ __device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, cons
             bits &= bits - 1;
             const int kp = 64 * word + b;
             const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
-            walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
+            if constexpr (V::kProbe && !DIAG) {
+                walk_group_pipelined<W>(v, acc, c, pv, g, lane, hq);
+            } else {
+                walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
+            }
         }
     } else {
 #pragma unroll
@@ -480,7 +568,11 @@ template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
                                           int lane, HitQueue& hq) {
     if (pv.n == 0) return;
-    walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane, hq);
+    if constexpr (V::kProbe && !DIAG) {
+        walk_group_pipelined<W>(v, acc, c, pv, 0, lane, hq);
+    } else {
+        walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane, hq);
+    }
 #pragma unroll
     for (int q = 0; q < W; ++q) walk_mask<W, DIAG>(v, acc, c, pv, c.w[q] & __ldg(pv.single_ne + q), q, -1, lane, hq);
 #pragma unroll

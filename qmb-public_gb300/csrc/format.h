@@ -39,7 +39,7 @@
 #include <stdint.h>
 
 #define QMBX_MAGIC 0x58424D51u  // "QMBX"
-#define QMBX_TABLE_VERSION 3u
+#define QMBX_TABLE_VERSION 4u
 #define QMBX_MAX_WORDS 4
 #define QMBX_ALIGN 256
 
@@ -47,8 +47,7 @@ enum { QMBX_PART_FWD = 0, QMBX_PART_ADJ = 1, QMBX_PART_DIAG = 2, QMBX_PARTS = 3 
 
 struct qmbx_table_part {
     int64_t n;            // terms in this part
-    uint64_t off_test;    // uint64[n][2W]  (mask, val) per word
-    uint64_t off_apply;   // uint64[n][2W]  (flip, par) per word
+    uint64_t off_term;    // uint64[n][W][4] (mask, val, flip, par) per word
     uint64_t off_coef;    // double[n][2]   sign-folded coefficient
     uint64_t off_coef32;  // float[n][4]    (re_hi, re_lo, im_hi, im_lo)
     uint64_t off_orig;    // int32[n]       index of the term in the input table

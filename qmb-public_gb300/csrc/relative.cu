@@ -93,9 +93,11 @@ struct RelativeVisitor : VisitorBase {
         acc.row = row;
         acc.hist = sh;
     }
-    __device__ __forceinline__ void candidate(Acc& acc, const Key<W>& img, const PartView& pv, int parity,
-                                              int64_t slot) const {
-        if (hash_find<W>(a.excl, img) >= 0) return;
+    static constexpr bool kProbe = true;
+    HashView lookup;  // the exclusion set
+    // A candidate record whose image is not excluded.
+    __device__ __forceinline__ void record(Acc& acc, const Key<W>& img, const PartView& pv, int parity,
+                                           int64_t slot) const {
         const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
         if (!EMIT) {
             atomicAdd(&acc.hist[b], 1);
@@ -115,11 +117,16 @@ struct RelativeVisitor : VisitorBase {
 #pragma unroll
         for (int q = 0; q < W; ++q) a.emit_keys[at * W + q] = img.w[q];
     }
+    __device__ __forceinline__ bool take(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
+                                         int64_t pos, int2&) const {
+        if (pos < 0) record(acc, img, a.off, parity, slot);
+        return false;
+    }
     __device__ __forceinline__ void visit(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        candidate(acc, img, a.off, parity, slot);
+        if (hash_find<W>(lookup, img) < 0) record(acc, img, a.off, parity, slot);
     }
     __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
-        candidate(acc, c, a.diag, parity, slot);
+        if (hash_find<W>(lookup, c) < 0) record(acc, c, a.diag, parity, slot);
     }
     __device__ __forceinline__ void reduce(Acc&) const {}
     __device__ __forceinline__ void finish(Acc&, int64_t, const Key<W>&) const {}
@@ -129,6 +136,7 @@ template <int W, bool EMIT>
 int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, cudaStream_t s) {
     RelativeVisitor<W, EMIT> v;
     v.a = r;
+    v.lookup = r.excl;
     KeyRows<W> src{keys_i};
     if (r.off.n >= kGroupedMinTerms) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
@@ -343,7 +351,8 @@ __global__ void es_factor_kernel(const double2* __restrict__ coef, const int32_t
 
 template <int W>
 struct SingleVisitor : VisitorBase {
-    HashView set;
+    static constexpr bool kProbe = true;
+    HashView lookup;  // the input rows
     const double* kf;
     const int32_t* orig;
     uint8_t* out;
@@ -359,12 +368,24 @@ struct SingleVisitor : VisitorBase {
 #pragma unroll
         for (int q = 0; q < W; ++q) a.best.w[q] = 0;
     }
+    __device__ __forceinline__ bool take(Acc& a, const Key<W>&, const Key<W>& img, int, int64_t slot, int64_t pos,
+                                         int2&) const {
+        if (pos >= 0) return false;
+        const double key = __ldg(kf + slot);
+        const int32_t t = __ldg(orig + slot);
+        if (a.term < 0 || key > a.key || (key == a.key && t < a.term)) {
+            a.key = key;
+            a.term = t;
+            a.best = img;
+        }
+        return false;
+    }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>&, const Key<W>& img, int, int64_t slot) const {
-        double key = __ldg(kf + slot);
-        int32_t t = __ldg(orig + slot);
-        bool better = a.term < 0 || key > a.key || (key == a.key && t < a.term);
+        const double key = __ldg(kf + slot);
+        const int32_t t = __ldg(orig + slot);
+        const bool better = a.term < 0 || key > a.key || (key == a.key && t < a.term);
         if (!better) return;
-        if (hash_find<W>(set, img) >= 0) return;
+        if (hash_find<W>(lookup, img) >= 0) return;
         a.key = key;
         a.term = t;
         a.best = img;

@@ -143,10 +143,8 @@ void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     p.n = n;
     p.n_groups = qmbx_group_count(words);
     uint64_t un = (uint64_t)n;
-    p.off_test = cursor;
-    cursor = align_up(cursor + un * 2 * words * 8);
-    p.off_apply = cursor;
-    cursor = align_up(cursor + un * 2 * words * 8);
+    p.off_term = cursor;
+    cursor = align_up(cursor + un * 4 * words * 8);
     p.off_coef = cursor;
     cursor = align_up(cursor + un * 16);
     p.off_coef32 = cursor;
@@ -256,13 +254,12 @@ void count_terms(const int16_t* site, const uint8_t* kind, int64_t n_terms, int3
 
 void write_term(char* blob, const qmbx_table_part& p, int words, int64_t slot, const Compiled& c, const double* coef,
                 int64_t orig) {
-    uint64_t* test = reinterpret_cast<uint64_t*>(blob + p.off_test) + slot * 2 * words;
-    uint64_t* apply = reinterpret_cast<uint64_t*>(blob + p.off_apply) + slot * 2 * words;
+    uint64_t* rec = reinterpret_cast<uint64_t*>(blob + p.off_term) + slot * 4 * words;
     for (int w = 0; w < words; ++w) {
-        test[2 * w + 0] = c.mask[w];
-        test[2 * w + 1] = c.val[w];
-        apply[2 * w + 0] = c.flip[w];
-        apply[2 * w + 1] = c.par[w];
+        rec[4 * w + 0] = c.mask[w];
+        rec[4 * w + 1] = c.val[w];
+        rec[4 * w + 2] = c.flip[w];
+        rec[4 * w + 3] = c.par[w];
     }
     double re = coef[0], im = coef[1];
     if (c.pconst) {
