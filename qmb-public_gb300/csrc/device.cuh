@@ -480,7 +480,7 @@ __device__ __forceinline__ int64_t hash_resolve(const HashView& h, const Key<W>&
 // hash slots are loaded together, so each lane keeps several independent
 // L2 requests in flight; v.take() sees each applicable term with the
 // lookup's answer.
-constexpr int kPipe = 4;
+constexpr int kPipe = 2;
 
 template <int W, class V>
 __device__ __forceinline__ void walk_group_pipelined(const V& v, typename V::Acc& acc, const Key<W>& c,
@@ -533,17 +533,80 @@ __device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& a
     }
 }
 
-// Visit the groups named by the set bits of a 64-bit mask (key positions
-// 64 * word + bit), as single groups (first < 0) or pair groups with first.
+// The pivot groups a row can reach, in a fixed order: group 0, the single
+// groups of its occupied positions, then for every occupied position p the
+// pair groups (p, q) with q occupied.  Warp-uniform state; next() yields one
+// group id at a time so the walk has a single call site (small code, few
+// registers).
+template <int W>
+struct GroupCursor {
+    const Key<W>* c;
+    const uint64_t* single_ne;
+    const uint64_t* pair_ne;
+    int first;        // -2: group 0 pending; -1: single level; >= 0: pair level with this first position
+    int word;         // word of the partner mask being drained
+    uint64_t bits;    // partner bits still to yield in `word`
+    uint64_t occ[W];  // occupied positions not yet used as `first`
+
+    __device__ __forceinline__ void start(const Key<W>& row, const PartView& pv) {
+        c = &row;
+        single_ne = pv.single_ne;
+        pair_ne = pv.pair_ne;
+        first = -2;
+        word = 0;
+        bits = 0;
+#pragma unroll
+        for (int q = 0; q < W; ++q) occ[q] = row.w[q];
+    }
+    __device__ __forceinline__ uint64_t partners(int r) const {
+        return c->w[r] & (first < 0 ? __ldg(single_ne + r) : __ldg(pair_ne + (int64_t)first * W + r));
+    }
+    __device__ __forceinline__ bool next(int64_t& g) {
+        if (first == -2) {
+            first = -1;
+            word = 0;
+            bits = partners(0);
+            g = 0;
+            return true;
+        }
+#pragma unroll 1
+        for (;;) {
+            if (bits) {
+                const int b = __ffsll((long long)bits) - 1;
+                bits &= bits - 1;
+                const int kp = 64 * word + b;
+                g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
+                return true;
+            }
+            if (word + 1 < W) {
+                ++word;
+                bits = partners(word);
+                continue;
+            }
+            // next first position (pair level)
+            int q = 0;
+#pragma unroll 1
+            while (q < W && occ[q] == 0) ++q;
+            if (q == W) return false;
+            const int b = __ffsll((long long)occ[q]) - 1;
+            occ[q] &= occ[q] - 1;
+            first = 64 * q + b;
+            word = q;  // partners sit at higher positions
+            bits = partners(word);
+        }
+    }
+};
+
 template <int W, bool DIAG, class V>
-__device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                          uint64_t bits, int word, int first, int lane, HitQueue& hq) {
+__device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
+                                          int lane, HitQueue& hq) {
+    if (pv.n == 0) return;
+    GroupCursor<W> cur;
+    cur.start(c, pv);
+    int64_t g;
     if (pv.wide) {
-        while (bits) {
-            const int b = __ffsll((long long)bits) - 1;
-            bits &= bits - 1;
-            const int kp = 64 * word + b;
-            const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
+#pragma unroll 1
+        while (cur.next(g)) {
             if constexpr (V::kProbe && !DIAG) {
                 walk_group_pipelined<W>(v, acc, c, pv, g, lane, hq);
             } else {
@@ -551,44 +614,14 @@ __device__ __forceinline__ void walk_mask(const V& v, typename V::Acc& acc, cons
             }
         }
     } else {
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const uint32_t chunk = (uint32_t)(bits >> (32 * half));
-            if ((chunk >> lane) & 1u) {
-                const int kp = 64 * word + 32 * half + lane;
-                const int64_t g = first < 0 ? qmbx_single_group(kp) : qmbx_pair_group(W, first, kp);
-                walk_group_serial<W, DIAG>(v, acc, c, pv, g);
-            }
+        // small groups: lane k takes every 32nd group of the sequence
+        int k = 0;
+#pragma unroll 1
+        while (cur.next(g)) {
+            if (k == lane) walk_group_serial<W, DIAG>(v, acc, c, pv, g);
+            k = (k + 1) & 31;
         }
         __syncwarp();
-    }
-}
-
-template <int W, bool DIAG, class V>
-__device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                          int lane, HitQueue& hq) {
-    if (pv.n == 0) return;
-    if constexpr (V::kProbe && !DIAG) {
-        walk_group_pipelined<W>(v, acc, c, pv, 0, lane, hq);
-    } else {
-        walk_group_lanes<W, DIAG>(v, acc, c, pv, 0, lane, hq);
-    }
-#pragma unroll
-    for (int q = 0; q < W; ++q) walk_mask<W, DIAG>(v, acc, c, pv, c.w[q] & __ldg(pv.single_ne + q), q, -1, lane, hq);
-#pragma unroll
-    for (int q = 0; q < W; ++q) {
-        uint64_t occ = c.w[q];
-        while (occ) {
-            const int b = __ffsll((long long)occ) - 1;
-            occ &= occ - 1;
-            const int kp = 64 * q + b;
-            const uint64_t* pn = pv.pair_ne + (int64_t)kp * W;
-#pragma unroll
-            for (int r = 0; r < W; ++r) {
-                if (r < q) continue;  // partners sit at higher key positions
-                walk_mask<W, DIAG>(v, acc, c, pv, c.w[r] & __ldg(pn + r), r, kp, lane, hq);
-            }
-        }
     }
 }
 
