@@ -38,6 +38,16 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 WORKLOADS = {
+    "c3": dict(n_orbit=26, n_alpha=7, n_beta=7, n_i=65536, n_j=65536, count_selected=0, seed=2025,
+               description="ab-initio 52 spin orbitals (n_qubytes 7), 7a+7b, 65536 configs, MLP 4x512 wave function, "
+                           "energy forward + backward"),
+    "c4": dict(hubbard=(8, 8, 1.0, 4.0), n_orbit=64, n_alpha=32, n_beta=32, n_i=1000000, n_j=1000000,
+               count_selected=0, seed=2026,
+               description="Fermi-Hubbard 8x8 open, t=1, U=4, 128 spin orbitals (n_qubytes 16), 32a+32b, "
+                           "1,000,000 configs, complex64 amplitudes"),
+    "c5": dict(n_orbit=38, n_alpha=10, n_beta=10, n_i=8192, n_j=8192, count_selected=1000000, seed=2027,
+               description="ab-initio 76 spin orbitals (n_qubytes 10), 10a+10b, 8192 seeds, find_relative top "
+                           "1,000,000"),
     "c2": dict(n_orbit=14, n_alpha=5, n_beta=5, n_i=20000, n_j=200000, count_selected=50000, seed=2024,
                description="ab-initio 28 spin orbitals (n_qubytes 4), 5a+5b, N_i 20000, N_j 200000, K 50000"),
     "c1": dict(n_orbit=6, n_alpha=3, n_beta=3, n_i=400, n_j=400, count_selected=100, seed=2024,
@@ -60,9 +70,15 @@ def make_workload(name: str):
     qmb = importlib.import_module("qmb-public_gb300")
     terms = qmb.terms
     w = WORKLOADS[name]
-    site, kind, coef = terms.integral_hamiltonian_tables(w["n_orbit"], seed=w["seed"])
+    if "hubbard" in w:
+        site, kind, coef = terms.sort_terms(*terms.prepare(terms.hubbard_dict(*w["hubbard"])))
+    else:
+        site, kind, coef = terms.integral_hamiltonian_tables(w["n_orbit"], seed=w["seed"])
     if w["n_i"] == w["n_j"] and name == "c1":
         ci = terms.all_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"])
+        cj = ci
+    elif w["n_i"] == w["n_j"]:
+        ci = terms.random_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"], w["n_i"], seed=w["seed"] + 1)
         cj = ci
     else:
         ci = terms.random_determinants(w["n_orbit"], w["n_alpha"], w["n_beta"], w["n_i"], seed=w["seed"] + 1)
@@ -134,7 +150,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -356,6 +372,135 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     return line
 
 
+class _Mlp:
+    """Plain MLP wave function: unpacked bits -> 4 hidden layers of 512 (SiLU) -> (log|psi|, phase), FP32."""
+
+    def __init__(self, n_sites: int, device, seed: int):
+        import torch
+
+        gen = torch.Generator().manual_seed(seed)
+        layers = []
+        width = n_sites
+        for _ in range(4):
+            lin = torch.nn.Linear(width, 512)
+            torch.nn.init.normal_(lin.weight, std=1.0 / math.sqrt(width), generator=gen)
+            torch.nn.init.zeros_(lin.bias)
+            layers += [lin, torch.nn.SiLU()]
+            width = 512
+        head = torch.nn.Linear(512, 2)
+        torch.nn.init.normal_(head.weight, std=0.01, generator=gen)
+        torch.nn.init.zeros_(head.bias)
+        layers.append(head)
+        self.net = torch.nn.Sequential(*layers).to(device)
+        self.n_sites = n_sites
+
+    def __call__(self, configs):
+        import torch
+
+        bitspack = importlib.import_module("qmb-public_gb300.bitspack")
+        bits = bitspack.unpack_int(configs, 1, self.n_sites).to(torch.float32)
+        out = self.net(bits)
+        return torch.polar(torch.exp(out[:, 0]), out[:, 1])
+
+
+def _timed_loop(fn, steps, device, flush=None):
+    import torch
+
+    stream = torch.cuda.current_stream(device)
+    pairs = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        pairs.append((a, b))
+    torch.cuda.synchronize(device)
+    return sum(a.elapsed_time(b) for a, b in pairs) / steps
+
+
+def run_extra(args, wl) -> dict:
+    """The other benchmark shapes: c3 (energy + gradient through an MLP), c4 (Hubbard 1M), c5 (find_relative 1M)."""
+    import torch
+
+    qmb = importlib.import_module("qmb-public_gb300")
+    native = importlib.import_module("qmb-public_gb300._native")
+    device = torch.device("cuda", 0)
+    kind = "fermi"
+    ham = qmb.Hamiltonian((torch.from_numpy(wl["site"]), torch.from_numpy(wl["kind"]), torch.from_numpy(wl["coef"])),
+                          kind=kind)
+    ci = torch.from_numpy(wl["configs_i"]).to(device)
+    T, nq, n = wl["n_terms"], wl["nq"], ci.shape[0]
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    line = {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": T, "n_rows": n, "n_qubytes": nq}
+    if args.workload == "c3":
+        mlp = _Mlp(8 * nq, device, seed=wl["spec"]["seed"])
+
+        def step(dtype):
+            for p in mlp.net.parameters():
+                p.grad = None
+            psi = mlp(ci)
+            e = qmb.variational_energy(ham, ci, psi if dtype == torch.complex64 else psi.to(torch.complex128))
+            e.backward()
+            return e
+
+        for _ in range(args.warmup):
+            step(torch.complex64)
+            step(torch.complex128)
+        native.profile_enable(True)
+        ms32 = _timed_loop(lambda: step(torch.complex64), args.steps, device, flush)
+        prof = native.profile_read()
+        native.profile_enable(False)
+        ms64 = _timed_loop(lambda: step(torch.complex128), args.steps, device, flush)
+        e32 = float(step(torch.complex64))
+        e64 = float(step(torch.complex128))
+        line.update({"metric": "energy forward + backward step (FP32-compensated)", "value": ms32, "unit": "ms",
+                     "higher_is_better": False, "fp64_ms": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),
+                     "apply_term_applications_per_s": 2 * T * n / (prof["groups"]["enumerate"][1] / args.steps * 1e-3),
+                     "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]}})
+    elif args.workload == "c4":
+        psi32 = torch.from_numpy(wl["psi"]).to(torch.complex64).to(device)
+        psi64 = psi32.to(torch.complex128)
+
+        def step32():
+            y = ham.apply_within_compensated(ci, psi32, ci)
+            return ham.apply_within_adjoint(ci, y.to(torch.complex64), ci)
+
+        def step64():
+            y = ham.apply_within(ci, psi64, ci)
+            return ham.apply_within_adjoint(ci, y, ci)
+
+        for _ in range(args.warmup):
+            step32()
+            step64()
+        ms32 = _timed_loop(step32, args.steps, device, flush)
+        ms64 = _timed_loop(step64, args.steps, device, flush)
+        e32 = float(qmb.variational_energy(ham, ci, psi32))
+        e64 = float(qmb.variational_energy(ham, ci, psi64))
+        line.update({"metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
+                     "value": 2 * T * n / (ms32 * 1e-3), "unit": "term-applications/s", "higher_is_better": True,
+                     "ms_per_step": ms32, "fp64_ms_per_step": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64)})
+    else:
+        psi = torch.from_numpy(wl["psi"]).to(device)
+        K = wl["spec"]["count_selected"]
+        rel = ham.find_relative(ci, psi, K)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rel = ham.find_relative(ci, psi, K)
+        torch.cuda.synchronize(device)
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        line.update({"metric": "find_relative wall time (top K of all connected records)", "value": ms, "unit": "ms",
+                     "higher_is_better": False, "count_selected": K, "rows_out": int(rel.shape[0]),
+                     "term_applications_per_s": T * n / (ms * 1e-3)})
+    line.update({"steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic"})
+    return line
+
+
 def run_reference(args, wl) -> dict:
     cpu = oracle_rate(wl, budget_s=args.cpu_seconds)
     value = cpu["value"]
@@ -402,6 +547,10 @@ def main():
 
     import torch
 
+    if args.workload in ("c3", "c4", "c5"):
+        if rank == 0:
+            print(json.dumps(run_extra(args, make_workload(args.workload))), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
 

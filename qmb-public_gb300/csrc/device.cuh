@@ -455,73 +455,6 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
     }
 }
 
-// hash_find split in two: the first slot is loaded by the caller (so that
-// several lookups can be in flight), the rest of the probe runs here.
-template <int W>
-__device__ __forceinline__ int64_t hash_resolve(const HashView& h, const Key<W>& key, uint64_t hv,
-                                                uint64_t first_slot) {
-    const uint32_t fp = (uint32_t)(hv >> 32);
-    uint64_t i = hv & h.mask;
-    uint64_t s = first_slot;
-    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
-        if (s == kEmptySlot) return -1;
-        if ((uint32_t)(s >> 32) == fp) {
-            const int64_t idx = (int64_t)(uint32_t)s;
-            if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
-        }
-        i = (i + 1) & h.mask;
-        s = __ldg(h.slots + i);
-    }
-    return -1;
-}
-
-// Walk one group with lanes over terms, kPipe terms per lane per step: the
-// term records of all kPipe are loaded, tested and hashed, then their first
-// hash slots are loaded together, so each lane keeps several independent
-// L2 requests in flight; v.take() sees each applicable term with the
-// lookup's answer.
-constexpr int kPipe = 2;
-
-template <int W, class V>
-__device__ __forceinline__ void walk_group_pipelined(const V& v, typename V::Acc& acc, const Key<W>& c,
-                                                     const PartView& pv, int64_t g, int lane, HitQueue& hq) {
-    const int2 se = __ldg(pv.groups + g);
-    for (int64_t base = se.x; base < se.y; base += 32 * kPipe) {
-        bool app[kPipe];
-        Key<W> img[kPipe];
-        int par[kPipe];
-        uint64_t hv[kPipe], s0[kPipe];
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) {
-            const int64_t t = base + 32 * k + lane;
-            app[k] = false;
-            par[k] = 0;
-            if (t < se.y) {
-                const TermRec<W> r = load_term<W>(pv, t);
-                app[k] = r.applies(c);
-                par[k] = r.image(c, img[k]);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) {
-            if (app[k]) {
-                hv[k] = key_hash<W>(img[k]);
-                s0[k] = __ldg(v.lookup.slots + (hv[k] & v.lookup.mask));
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) {
-            int2 h = make_int2(0, 0);
-            bool hit = false;
-            if (app[k]) {
-                const int64_t pos = hash_resolve<W>(v.lookup, img[k], hv[k], s0[k]);
-                hit = v.take(acc, c, img[k], par[k], base + 32 * k + lane, pos, h);
-            }
-            if constexpr (V::kBatched) queue_push(v, acc, hq, lane, hit, h);
-        }
-    }
-}
-
 // Walk one group entirely in this lane (hits processed at once).
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& acc, const Key<W>& c,
@@ -606,13 +539,7 @@ __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, cons
     int64_t g;
     if (pv.wide) {
 #pragma unroll 1
-        while (cur.next(g)) {
-            if constexpr (V::kProbe && !DIAG) {
-                walk_group_pipelined<W>(v, acc, c, pv, g, lane, hq);
-            } else {
-                walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
-            }
-        }
+        while (cur.next(g)) walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
     } else {
         // small groups: lane k takes every 32nd group of the sequence
         int k = 0;
