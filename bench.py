@@ -454,8 +454,8 @@ def run_extra(args, wl) -> dict:
         prof = native.profile_read()
         native.profile_enable(False)
         ms64 = _timed_loop(lambda: step(torch.complex128), args.steps, device, flush)
-        e32 = float(step(torch.complex64))
-        e64 = float(step(torch.complex128))
+        e32 = float(step(torch.complex64).detach())
+        e64 = float(step(torch.complex128).detach())
         line.update({"metric": "energy forward + backward step (FP32-compensated)", "value": ms32, "unit": "ms",
                      "higher_is_better": False, "fp64_ms": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
                      "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const
     v.block_init(sh);
     __syncthreads();
     typename V::Acc acc;
-    v.init(acc, row, c, sh);
+    if (live) v.init(acc, row, c, sh);  // init may read per-row data: never for padding lanes
     for (int part = 0; part < 2; ++part) {
         const PartView& pv = part == 0 ? off : diag;
         for (int64_t t0 = 0; t0 < pv.n; t0 += kTermTile) {
