@@ -168,6 +168,13 @@ struct GatherF64 : VisitorBase {
         }
         res[__ldg(unique + u)] = make_double2(a.re, a.im);
     }
+    // pivot-major walks: one (row, group) partial, added atomically; the
+    // diagonal part is applied by a separate pass
+    __device__ __forceinline__ void flush(Acc& a, int64_t u, const Key<W>&) const {
+        double2* r = res + __ldg(unique + u);
+        if (a.re != 0.0) atomicAdd(&r->x, a.re);
+        if (a.im != 0.0) atomicAdd(&r->y, a.im);
+    }
 };
 
 template <int W, bool CONJ>
@@ -230,6 +237,12 @@ struct GatherF32C : VisitorBase {
             }
         }
         res[__ldg(unique + u)] = make_double2(re, im);
+    }
+    __device__ __forceinline__ void flush(Acc& a, int64_t u, const Key<W>&) const {
+        const double re = a.re.value(), im = a.im.value();
+        double2* r = res + __ldg(unique + u);
+        if (re != 0.0) atomicAdd(&r->x, re);
+        if (im != 0.0) atomicAdd(&r->y, im);
     }
 };
 
@@ -349,6 +362,53 @@ struct Scatter : VisitorBase {
     }
 };
 
+// Diagonal terms of a pivot-major walk: per walked row, the sum of its
+// diagonal coefficients times the amplitude of the row itself, added to the
+// row's result (gather: amplitude from the input side; scatter: the walked
+// amplitude, result at the output side's copy of the row).
+template <int W, bool CONJ, bool F32, bool SCATTER>
+struct DiagAdd : VisitorBase {
+    HashView lookup;
+    const void* val;
+    const int32_t* unique;
+    const double2* dcoef;
+    double2* res;
+    struct Acc {
+        double dre, dim;
+    };
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.dre = a.dim = 0.0; }
+    __device__ __forceinline__ void visit(Acc&, const Key<W>&, const Key<W>&, int, int64_t) const {}
+    __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
+        const double2 cf = __ldg(dcoef + slot);
+        const double ci = CONJ ? -cf.y : cf.y;
+        a.dre += parity ? -cf.x : cf.x;
+        a.dim += parity ? -ci : ci;
+    }
+    __device__ __forceinline__ void reduce(Acc& a) const {
+        a.dre = warp_sum(a.dre);
+        a.dim = warp_sum(a.dim);
+    }
+    __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
+        if (a.dre == 0.0 && a.dim == 0.0) return;
+        const int64_t pos = hash_find<W>(lookup, c);
+        if (pos < 0) return;
+        const int64_t from = SCATTER ? (int64_t)__ldg(unique + u) : pos;
+        const int64_t to = SCATTER ? pos : (int64_t)__ldg(unique + u);
+        double px, py;
+        if (F32) {
+            const float2 q = __ldg(static_cast<const float2*>(val) + from);
+            px = q.x;
+            py = q.y;
+        } else {
+            const double2 q = __ldg(static_cast<const double2*>(val) + from);
+            px = q.x;
+            py = q.y;
+        }
+        atomicAdd(&res[to].x, a.dre * px - a.dim * py);
+        atomicAdd(&res[to].y, a.dre * py + a.dim * px);
+    }
+};
+
 // Write the user's output rows from the per-first-row results: the forward
 // map gives each key's value to its first row only (repeated rows get zero),
 // the adjoint gives it to every row holding the key.
@@ -419,6 +479,23 @@ int launch_walk(const V& v, const HashRows& walk, const PartView& part, const Pa
     return QMBX_OK;
 }
 
+// Pivot-major walk of the changing terms (results added into res by the
+// visitor's flush or hits) followed by a tiled pass over the diagonal terms.
+template <int W, class V, class D>
+int launch_pivot(const V& v, const D& dv, const HashRows& walk, const PartView& part, const PartView& diag,
+                 cudaStream_t s) {
+    UniqueRows<W> src{walk.keys, walk.unique};
+    QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, walk.count, walk.n, part));
+    QMBX_LAUNCH_CHECK("apply_within pivot walk");
+    if (diag.n > 0) {
+        PartView none = part;
+        none.n = 0;
+        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+        QMBX_LAUNCH_CHECK("apply_within diagonal pass");
+    }
+    return QMBX_OK;
+}
+
 // Forward maps amplitudes on configs_i (input side) to configs_j (output
 // side); the adjoint maps configs_j to configs_i.  Gather walks the output
 // side's distinct rows (daggered terms for the forward map) and sums in
@@ -474,49 +551,68 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     const bool include_diag = a.prec == Prec::F64 || a.include_diag;
     if (!include_diag) diag.n = 0;
     const bool scatter = !a.same && 2 * n_in < n_out;
+    // walk the input side (scatter) with forward terms for the forward map
+    // or daggered terms (conjugated) for the adjoint; walk the output side
+    // (gather) with daggered terms for the forward map or forward terms
+    // (conjugated) for the adjoint
+    const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
+    const bool pivot = part.n >= kGroupedMinTerms;
+    if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     if (scatter) {
-        // walk the input side: forward terms for the forward map, daggered
-        // terms (conjugated) for the adjoint
-        const PartView& part = a.adjoint ? adj : fwd;
-        QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
         const HashView look = out_set.hash();
+#define QMBX_SCATTER_CASE(CONJ, F32)                                                                               \
+    {                                                                                                              \
+        Scatter<W, CONJ, F32> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res}; \
+        if (pivot) {                                                                                               \
+            DiagAdd<W, CONJ, F32, true> dv{{}, look, val, in_set.unique, diag.coef, res};                          \
+            st = launch_pivot<W>(v, dv, in_set, part, diag, s);                                                    \
+        } else {                                                                                                   \
+            st = launch_walk<W>(v, in_set, part, diag, s);                                                         \
+        }                                                                                                          \
+    }
         if (a.prec == Prec::F64) {
-            if (a.adjoint) {
-                Scatter<W, true, false> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, 1, res};
-                st = launch_walk<W>(v, in_set, part, diag, s);
-            } else {
-                Scatter<W, false, false> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, 1, res};
-                st = launch_walk<W>(v, in_set, part, diag, s);
-            }
+            if (a.adjoint) QMBX_SCATTER_CASE(true, false) else QMBX_SCATTER_CASE(false, false)
         } else {
-            if (a.adjoint) {
-                Scatter<W, true, true> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res};
-                st = launch_walk<W>(v, in_set, part, diag, s);
-            } else {
-                Scatter<W, false, true> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res};
-                st = launch_walk<W>(v, in_set, part, diag, s);
-            }
+            if (a.adjoint) QMBX_SCATTER_CASE(true, true) else QMBX_SCATTER_CASE(false, true)
         }
+#undef QMBX_SCATTER_CASE
     } else {
-        // gather: walk the output side with daggered terms for the forward
-        // map, forward terms (conjugated) for the adjoint
-        const PartView& part = a.adjoint ? fwd : adj;
         const HashView look = in_set.hash();
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
                 GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
-                st = launch_walk<W>(v, out_set, part, diag, s);
+                if (pivot) {
+                    DiagAdd<W, true, false, false> dv{{}, look, val, out_set.unique, diag.coef, res};
+                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
+                } else {
+                    st = launch_walk<W>(v, out_set, part, diag, s);
+                }
             } else {
                 GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
-                st = launch_walk<W>(v, out_set, part, diag, s);
+                if (pivot) {
+                    DiagAdd<W, false, false, false> dv{{}, look, val, out_set.unique, diag.coef, res};
+                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
+                } else {
+                    st = launch_walk<W>(v, out_set, part, diag, s);
+                }
             }
         } else {
             if (a.adjoint) {
                 GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
-                st = launch_walk<W>(v, out_set, part, diag, s);
+                if (pivot) {
+                    DiagAdd<W, true, true, false> dv{{}, look, val, out_set.unique, diag.coef, res};
+                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
+                } else {
+                    st = launch_walk<W>(v, out_set, part, diag, s);
+                }
             } else {
                 GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
-                st = launch_walk<W>(v, out_set, part, diag, s);
+                if (pivot) {
+                    DiagAdd<W, false, true, false> dv{{}, look, val, out_set.unique, diag.coef, res};
+                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
+                } else {
+                    st = launch_walk<W>(v, out_set, part, diag, s);
+                }
             }
         }
     }

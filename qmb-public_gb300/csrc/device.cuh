@@ -146,6 +146,8 @@ struct PartView {
     const int2* groups;        // [start, end) of every pivot group
     const uint64_t* single_ne; // [W]
     const uint64_t* pair_ne;   // [64W][W]
+    const int4* nonempty;      // (start, end, p, q) of the non-empty groups
+    int64_t n_nonempty;
     int64_t n;
     int wide;                  // groups are large: walk each with lanes over its terms
 };
@@ -163,6 +165,8 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
     v.groups = reinterpret_cast<const int2*>(base + p.off_groups);
     v.single_ne = reinterpret_cast<const uint64_t*>(base + p.off_single_ne);
     v.pair_ne = reinterpret_cast<const uint64_t*>(base + p.off_pair_ne);
+    v.nonempty = reinterpret_cast<const int4*>(base + p.off_nonempty);
+    v.n_nonempty = p.n_nonempty;
     v.n = p.n;
     v.wide = p.wide_groups;
     return v;
@@ -266,6 +270,8 @@ __device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, co
 // Defaults for the optional parts of the visitor protocol: no shared memory,
 // no per-block set-up or flush.
 struct VisitorBase {
+    template <class Acc, class K>
+    __device__ __forceinline__ void flush(Acc&, int64_t, const K&) const {}
     static constexpr int kShared = 0;
     static constexpr bool kBatched = false;  // hits are queued and processed by apply_hit with full lanes
     static constexpr bool kProbe = false;    // has `HashView lookup` and take(): lookups are pipelined
@@ -577,6 +583,124 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
     __syncthreads();
     v.block_flush(sh);
 }
+
+// ---------------------------------------------------------------------------
+// the pivot-major enumeration kernel.  A work item is one non-empty pivot
+// group and a chunk of kPivotRows rows: the block scans the chunk for the
+// rows that occupy the group's pivot positions, stages the group's terms in
+// shared memory (slice by slice when they do not fit) and walks them for
+// every matching row, one warp per row with lanes over terms.  Term data is
+// read once per item from L2 and then from shared memory; only the lookups
+// of images go to L2.  Each (row, group) result is handed to v.flush().
+// ---------------------------------------------------------------------------
+
+constexpr int kPivotTermBytes = 32768;
+constexpr int kPivotRows = 2048;
+
+template <int W>
+__device__ __forceinline__ bool has_position(const Key<W>& c, int kp) {
+    if (kp < 0) return true;
+    uint64_t w = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) w = (q == (kp >> 6)) ? c.w[q] : w;
+    return (w >> (kp & 63)) & 1ull;
+}
+
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int* __restrict__ n_rows, int64_t n_max,
+                                                         PartView pv) {
+    // the visitor's own shared memory comes out of the term staging area, so
+    // the block stays within the 48 KB of static shared memory
+    constexpr int kTerms = (kPivotTermBytes - 4 * V::kShared) / (32 * W);
+    __shared__ __align__(16) uint64_t s_terms[kTerms * 4 * W];
+    __shared__ int32_t s_rows[kPivotRows];
+    __shared__ int s_nrows;
+    __shared__ int2 hitq[kWarpsPerBlock][64];
+    __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
+    v.block_init(sh);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
+    const int64_t chunks = (n + kPivotRows - 1) / kPivotRows;
+    const int64_t items = pv.n_nonempty * chunks;
+    for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const int64_t gi = item / chunks;
+        const int64_t r0 = (item - gi * chunks) * kPivotRows;
+        const int64_t r1 = r0 + kPivotRows < n ? r0 + kPivotRows : n;
+        const int4 grp = __ldg(pv.nonempty + gi);
+        if (threadIdx.x == 0) s_nrows = 0;
+        __syncthreads();
+        // rows of the chunk that occupy the pivot positions
+        for (int64_t base = r0; base < r1; base += kThreads) {
+            const int64_t r = base + threadIdx.x;
+            bool m = false;
+            if (r < r1) {
+                const Key<W> c = src.get(r);
+                m = has_position<W>(c, grp.z) && has_position<W>(c, grp.w);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, m);
+            int at = 0;
+            if (lane == 0 && bal) at = atomicAdd(&s_nrows, __popc(bal));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (m) s_rows[at + __popc(bal & lt)] = (int32_t)(r - r0);
+        }
+        __syncthreads();
+        const int nrows = s_nrows;
+        if (nrows > 0) {
+            for (int ts = grp.x; ts < grp.y; ts += kTerms) {
+                const int cnt = grp.y - ts < kTerms ? grp.y - ts : kTerms;
+                __syncthreads();
+                const ulonglong2* from = reinterpret_cast<const ulonglong2*>(pv.term + (int64_t)ts * 4 * W);
+                ulonglong2* to = reinterpret_cast<ulonglong2*>(s_terms);
+                for (int k = threadIdx.x; k < cnt * 2 * W; k += kThreads) to[k] = __ldg(from + k);
+                __syncthreads();
+                for (int i = warp; i < nrows; i += kWarpsPerBlock) {
+                    const int64_t u = r0 + s_rows[i];
+                    const Key<W> c = src.get(u);
+                    typename V::Acc acc;
+                    v.init(acc, u, c, sh);
+                    HitQueue hq{hitq[warp], 0};
+                    for (int b = 0; b < cnt; b += 32) {
+                        const int k = b + lane;
+                        int2 h = make_int2(0, 0);
+                        bool hit = false;
+                        if (k < cnt) {
+                            TermRec<W> rec;
+                            const ulonglong2* sp = reinterpret_cast<const ulonglong2*>(s_terms + (int64_t)k * 4 * W);
+#pragma unroll
+                            for (int q = 0; q < 2 * W; ++q) {
+                                const ulonglong2 x = sp[q];
+                                rec.m[2 * q] = x.x;
+                                rec.m[2 * q + 1] = x.y;
+                            }
+                            if (rec.applies(c)) {
+                                Key<W> img;
+                                const int par = rec.image(c, img);
+                                if constexpr (V::kBatched) {
+                                    hit = v.probe(acc, c, img, par, ts + k, h);
+                                } else {
+                                    v.visit(acc, c, img, par, ts + k);
+                                }
+                            }
+                        }
+                        if constexpr (V::kBatched) queue_push(v, acc, hq, lane, hit, h);
+                    }
+                    if constexpr (V::kBatched) queue_drain(v, acc, hq, lane, true);
+                    v.reduce(acc);
+                    if (lane == 0) v.flush(acc, u, c);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    v.block_flush(sh);
+}
+
+// Grid for pivot_kernel: a few resident blocks per SM, looping over work items.
+int pivot_grid();
 
 // Grid for grouped_kernel: enough warps for every row, at most a few waves.
 int grouped_grid(int64_t n_rows);

@@ -39,7 +39,7 @@
 #include <stdint.h>
 
 #define QMBX_MAGIC 0x58424D51u  // "QMBX"
-#define QMBX_TABLE_VERSION 4u
+#define QMBX_TABLE_VERSION 5u
 #define QMBX_MAX_WORDS 4
 #define QMBX_ALIGN 256
 
@@ -55,6 +55,8 @@ struct qmbx_table_part {
     uint64_t off_groups;  // int32[n_groups][2]  [start, end) of each group
     uint64_t off_single_ne;  // uint64[W]       non-empty single groups by key position
     uint64_t off_pair_ne;    // uint64[64W][W]  for position p: positions q > p with a non-empty pair group
+    uint64_t off_nonempty;   // int32[n_groups][4]: (start, end, p, q) of each non-empty group in id order
+                             // (p, q the pivot key positions, -1 when absent; first n_nonempty rows valid)
     int64_t n_groups;        // 1 + 64W + 64W(64W-1)/2
     int64_t n_nonempty;      // groups holding at least one term
     int32_t wide_groups;     // 1 when non-empty groups hold 8 or more terms on average

@@ -528,6 +528,20 @@ QMBX_INSTANTIATE_KEYS(4)
 
 namespace qmbx {
 
+static int sm_count() {
+    static int sms[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    if (sms[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
+        sms[dev] = v;
+    }
+    return sms[dev];
+}
+
+int pivot_grid() { return sm_count() * 4; }
+
 int grouped_grid(int64_t n_rows) {
     static int sms[64] = {0};
     int dev = 0;

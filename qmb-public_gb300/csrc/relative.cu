@@ -139,7 +139,13 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
     v.lookup = r.excl;
     KeyRows<W> src{keys_i};
     if (r.off.n >= kGroupedMinTerms) {
-        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
+        // pivot-major walk of the changing terms, then the diagonal terms tiled
+        QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off));
+        if (r.diag.n > 0) {
+            PartView none = r.off;
+            none.n = 0;
+            QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, none, r.diag));
+        }
     } else {
         QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
     }

@@ -159,6 +159,8 @@ void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     cursor = align_up(cursor + (uint64_t)words * 8);
     p.off_pair_ne = cursor;
     cursor = align_up(cursor + (uint64_t)64 * words * words * 8);
+    p.off_nonempty = cursor;
+    cursor = align_up(cursor + (uint64_t)p.n_groups * 16);
 }
 
 // Pivot group of a compiled term (see format.h).
@@ -193,23 +195,33 @@ void group_part(char* blob, qmbx_table_part& p, int words, const std::vector<int
     int32_t* groups = reinterpret_cast<int32_t*>(blob + p.off_groups);
     uint64_t* single_ne = reinterpret_cast<uint64_t*>(blob + p.off_single_ne);
     uint64_t* pair_ne = reinterpret_cast<uint64_t*>(blob + p.off_pair_ne);
+    int32_t* listed = reinterpret_cast<int32_t*>(blob + p.off_nonempty);
     int64_t nonempty = 0;
     const int P = 64 * words;
     for (int64_t g = 0; g < G; ++g) {
         groups[2 * g + 0] = (int32_t)count[(size_t)g];
         groups[2 * g + 1] = (int32_t)count[(size_t)g + 1];
         if (count[(size_t)g + 1] == count[(size_t)g]) continue;
-        ++nonempty;
+        int pivot_p = -1, pivot_q = -1;
         if (g >= 1 && g <= P) {
             int kp = (int)(g - 1);
             single_ne[kp >> 6] |= 1ull << (kp & 63);
+            pivot_p = kp;
         } else if (g > P) {
             int64_t r = g - 1 - P;  // q(q-1)/2 + p
             int q = 1;
             while ((int64_t)(q + 1) * q / 2 <= r) ++q;
             int pp = (int)(r - (int64_t)q * (q - 1) / 2);
             pair_ne[(size_t)pp * words + (q >> 6)] |= 1ull << (q & 63);
+            pivot_p = pp;
+            pivot_q = q;
         }
+        int32_t* row = listed + 4 * nonempty;
+        row[0] = (int32_t)count[(size_t)g];
+        row[1] = (int32_t)count[(size_t)g + 1];
+        row[2] = pivot_p;
+        row[3] = pivot_q;
+        ++nonempty;
     }
     p.n_nonempty = nonempty;
     p.wide_groups = (nonempty > 0 && p.n >= 8 * nonempty) ? 1 : 0;

@@ -45,7 +45,7 @@ def test_version_and_no_error(lib):
 class Part(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("off_term", ctypes.c_uint64), ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
                 ("off_norm", ctypes.c_uint64), ("off_groups", ctypes.c_uint64), ("off_single_ne", ctypes.c_uint64),
-                ("off_pair_ne", ctypes.c_uint64), ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
+                ("off_pair_ne", ctypes.c_uint64), ("off_nonempty", ctypes.c_uint64), ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
                 ("wide_groups", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
@@ -106,7 +106,18 @@ def check_groups(blob, h, which, part):
     assert groups[0, 0] == 0 and groups[-1, 1] == p.n
     assert np.all(groups[1:, 0] == groups[:-1, 1])
     P = 64 * w
-    for g in np.nonzero(groups[:, 1] > groups[:, 0])[0]:
+    listed = np.frombuffer(blob, dtype=np.int32, count=4 * p.n_nonempty, offset=p.off_nonempty).reshape(-1, 4)
+    nonempty = np.nonzero(groups[:, 1] > groups[:, 0])[0]
+    assert len(nonempty) == p.n_nonempty
+    assert np.array_equal(listed[:, :2], groups[nonempty])
+    for (lo, hi, a, b), g in zip(listed, nonempty):
+        if g == 0:
+            assert a == -1 and b == -1
+        elif g <= P:
+            assert a == g - 1 and b == -1
+        else:
+            assert g == 1 + P + b * (b - 1) // 2 + a and 0 <= a < b
+    for g in nonempty:
         lo, hi = groups[g]
         assert list(orig[lo:hi]) == sorted(orig[lo:hi])
         for slot in range(lo, hi):
