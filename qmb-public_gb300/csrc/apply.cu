@@ -362,6 +362,63 @@ struct Scatter : VisitorBase {
     }
 };
 
+// Hits of a pivot-major walk: each carries its walked row, and its product
+// is added at once to the output row with FP64 atomics (gather: the walked
+// row, amplitude of the looked-up row; scatter: the looked-up row,
+// amplitude of the walked row).  FP32 forms the products exactly in FP32
+// (two-products) and converts them to FP64 for the add.
+template <int W, bool CONJ, bool F32, bool SCATTER>
+struct PivotHits : VisitorBase {
+    static constexpr bool kStateless = true;
+    HashView lookup;
+    const void* val;        // amplitude per first row of the input side
+    const int32_t* unique;  // walked index -> first row
+    const double2* coef;
+    const float4* coef32;
+    double2* res;
+    struct Acc {};
+    __device__ __forceinline__ bool probe_row(const Key<W>&, const Key<W>& img, int parity, int64_t slot, int64_t u,
+                                              int4& h) const {
+        const int64_t pos = hash_find<W>(lookup, img);
+        if (pos < 0) return false;
+        h = make_int4((int)slot | (parity << 31), (int)pos, (int)u, 0);
+        return true;
+    }
+    __device__ __forceinline__ void apply_row_hit(int4 h) const {
+        const int64_t slot = h.x & 0x7fffffff;
+        const int64_t walked = __ldg(unique + h.z);
+        const int64_t from = SCATTER ? walked : (int64_t)h.y;
+        const int64_t to = SCATTER ? (int64_t)h.y : walked;
+        double re, im;
+        if (F32) {
+            const float4 cf = __ldg(coef32 + slot);
+            const float2 p = __ldg(static_cast<const float2*>(val) + from);
+            const float chi = CONJ ? -cf.z : cf.z, cli = CONJ ? -cf.w : cf.w;
+            float x1, e1, x2, e2;
+            two_prod(cf.x, p.x, x1, e1);
+            two_prod(chi, p.y, x2, e2);
+            float lo = __fadd_rn(__fsub_rn(e1, e2), __fsub_rn(__fmul_rn(cf.y, p.x), __fmul_rn(cli, p.y)));
+            re = ((double)x1 - (double)x2) + (double)lo;
+            two_prod(cf.x, p.y, x1, e1);
+            two_prod(chi, p.x, x2, e2);
+            lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fmul_rn(cf.y, p.y), __fmul_rn(cli, p.x)));
+            im = ((double)x1 + (double)x2) + (double)lo;
+        } else {
+            const double2 cf = __ldg(coef + slot);
+            const double2 p = __ldg(static_cast<const double2*>(val) + from);
+            const double ci = CONJ ? -cf.y : cf.y;
+            re = cf.x * p.x - ci * p.y;
+            im = cf.x * p.y + ci * p.x;
+        }
+        if (h.x < 0) {
+            re = -re;
+            im = -im;
+        }
+        atomicAdd(&res[to].x, re);
+        atomicAdd(&res[to].y, im);
+    }
+};
+
 // Diagonal terms of a pivot-major walk: per walked row, the sum of its
 // diagonal coefficients times the amplitude of the row itself, added to the
 // row's result (gather: amplitude from the input side; scatter: the walked
@@ -558,61 +615,64 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
     const bool pivot = part.n >= kGroupedMinTerms;
     if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
-    if (scatter) {
-        const HashView look = out_set.hash();
-#define QMBX_SCATTER_CASE(CONJ, F32)                                                                               \
-    {                                                                                                              \
-        Scatter<W, CONJ, F32> v{{}, look, val, in_set.unique, part.coef, part.coef32, diag.coef, include_diag, res}; \
-        if (pivot) {                                                                                               \
-            DiagAdd<W, CONJ, F32, true> dv{{}, look, val, in_set.unique, diag.coef, res};                          \
-            st = launch_pivot<W>(v, dv, in_set, part, diag, s);                                                    \
-        } else {                                                                                                   \
-            st = launch_walk<W>(v, in_set, part, diag, s);                                                         \
-        }                                                                                                          \
+    const HashRows& walk = scatter ? in_set : out_set;
+    const HashView look = scatter ? out_set.hash() : in_set.hash();
+    if (pivot) {
+#define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
+    {                                                                                                            \
+        PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res};             \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, res};                           \
+        st = launch_pivot<W>(v, dv, walk, part, diag, s);                                                        \
     }
-        if (a.prec == Prec::F64) {
-            if (a.adjoint) QMBX_SCATTER_CASE(true, false) else QMBX_SCATTER_CASE(false, false)
-        } else {
-            if (a.adjoint) QMBX_SCATTER_CASE(true, true) else QMBX_SCATTER_CASE(false, true)
-        }
-#undef QMBX_SCATTER_CASE
-    } else {
-        const HashView look = in_set.hash();
-        if (a.prec == Prec::F64) {
+        const bool f32 = a.prec == Prec::F32C;
+        if (scatter) {
             if (a.adjoint) {
-                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
-                if (pivot) {
-                    DiagAdd<W, true, false, false> dv{{}, look, val, out_set.unique, diag.coef, res};
-                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
-                } else {
-                    st = launch_walk<W>(v, out_set, part, diag, s);
-                }
+                if (f32) QMBX_PIVOT_CASE(true, true, true) else QMBX_PIVOT_CASE(true, false, true)
             } else {
-                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, out_set.unique, res};
-                if (pivot) {
-                    DiagAdd<W, false, false, false> dv{{}, look, val, out_set.unique, diag.coef, res};
-                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
-                } else {
-                    st = launch_walk<W>(v, out_set, part, diag, s);
-                }
+                if (f32) QMBX_PIVOT_CASE(false, true, true) else QMBX_PIVOT_CASE(false, false, true)
             }
         } else {
             if (a.adjoint) {
-                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
-                if (pivot) {
-                    DiagAdd<W, true, true, false> dv{{}, look, val, out_set.unique, diag.coef, res};
-                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
-                } else {
-                    st = launch_walk<W>(v, out_set, part, diag, s);
-                }
+                if (f32) QMBX_PIVOT_CASE(true, true, false) else QMBX_PIVOT_CASE(true, false, false)
             } else {
-                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, out_set.unique, res};
-                if (pivot) {
-                    DiagAdd<W, false, true, false> dv{{}, look, val, out_set.unique, diag.coef, res};
-                    st = launch_pivot<W>(v, dv, out_set, part, diag, s);
-                } else {
-                    st = launch_walk<W>(v, out_set, part, diag, s);
-                }
+                if (f32) QMBX_PIVOT_CASE(false, true, false) else QMBX_PIVOT_CASE(false, false, false)
+            }
+        }
+#undef QMBX_PIVOT_CASE
+    } else if (scatter) {
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            } else {
+                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            }
+        } else {
+            if (a.adjoint) {
+                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            } else {
+                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            }
+        }
+    } else {
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            } else {
+                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            }
+        } else {
+            if (a.adjoint) {
+                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
+            } else {
+                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
+                st = launch_walk<W>(v, walk, part, diag, s);
             }
         }
     }

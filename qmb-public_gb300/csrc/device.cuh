@@ -274,7 +274,7 @@ struct VisitorBase {
     __device__ __forceinline__ void flush(Acc&, int64_t, const K&) const {}
     static constexpr int kShared = 0;
     static constexpr bool kBatched = false;  // hits are queued and processed by apply_hit with full lanes
-    static constexpr bool kProbe = false;    // has `HashView lookup` and take(): lookups are pipelined
+    static constexpr bool kStateless = false; // pivot walks: hits carry their row and need no per-row state
     template <class Acc>
     __device__ __forceinline__ void apply_hit(Acc&, int2) const {}
     __device__ __forceinline__ void block_init(int*) const {}
@@ -615,13 +615,15 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
     __shared__ __align__(16) uint64_t s_terms[kTerms * 4 * W];
     __shared__ int32_t s_rows[kPivotRows];
     __shared__ int s_nrows;
-    __shared__ int2 hitq[kWarpsPerBlock][64];
+    __shared__ int4 hitq[kWarpsPerBlock][64];
     __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
     v.block_init(sh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
+    int4* hq = hitq[warp];
+    int hcount = 0;  // warp-uniform; the queue lives across rows and items
     const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
     const int64_t chunks = (n + kPivotRows - 1) / kPivotRows;
     const int64_t items = pv.n_nonempty * chunks;
@@ -660,11 +662,10 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
                     const int64_t u = r0 + s_rows[i];
                     const Key<W> c = src.get(u);
                     typename V::Acc acc;
-                    v.init(acc, u, c, sh);
-                    HitQueue hq{hitq[warp], 0};
+                    if constexpr (!V::kStateless) v.init(acc, u, c, sh);
                     for (int b = 0; b < cnt; b += 32) {
                         const int k = b + lane;
-                        int2 h = make_int2(0, 0);
+                        int4 h = make_int4(0, 0, 0, 0);
                         bool hit = false;
                         if (k < cnt) {
                             TermRec<W> rec;
@@ -678,22 +679,41 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
                             if (rec.applies(c)) {
                                 Key<W> img;
                                 const int par = rec.image(c, img);
-                                if constexpr (V::kBatched) {
-                                    hit = v.probe(acc, c, img, par, ts + k, h);
+                                if constexpr (V::kStateless) {
+                                    hit = v.probe_row(c, img, par, ts + k, u, h);
                                 } else {
                                     v.visit(acc, c, img, par, ts + k);
                                 }
                             }
                         }
-                        if constexpr (V::kBatched) queue_push(v, acc, hq, lane, hit, h);
+                        if constexpr (V::kStateless) {
+                            // queue the hit; 32 queued hits are applied with all lanes
+                            const unsigned m = __ballot_sync(0xffffffffu, hit);
+                            if (m) {
+                                if (hit) hq[hcount + __popc(m & lt)] = h;
+                                hcount += __popc(m);
+                                __syncwarp();
+                                if (hcount >= 32) {
+                                    v.apply_row_hit(hq[lane]);
+                                    __syncwarp();
+                                    if (lane < hcount - 32) hq[lane] = hq[32 + lane];
+                                    __syncwarp();
+                                    hcount -= 32;
+                                }
+                            }
+                        }
                     }
-                    if constexpr (V::kBatched) queue_drain(v, acc, hq, lane, true);
-                    v.reduce(acc);
-                    if (lane == 0) v.flush(acc, u, c);
+                    if constexpr (!V::kStateless) {
+                        v.reduce(acc);
+                        if (lane == 0) v.flush(acc, u, c);
+                    }
                 }
             }
         }
         __syncthreads();
+    }
+    if constexpr (V::kStateless) {
+        if (lane < hcount) v.apply_row_hit(hq[lane]);
     }
     __syncthreads();
     v.block_flush(sh);
