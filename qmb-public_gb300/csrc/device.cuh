@@ -115,20 +115,39 @@ struct HashView {
     uint64_t mask;         // slot count - 1 (a power of two minus one)
 };
 
-// Index of key among the unique keys, or -1.
+// Probing runs over 4-slot buckets (32 bytes, one L2 sector): a key's home
+// is the bucket its hash selects, and a lookup loads a whole bucket with two
+// 16-byte loads; with the table at most a quarter full it almost always ends
+// in the home bucket.  Inserts fill the same sequence slot by slot, so a
+// bucket with an empty slot ends an unsuccessful search.
+constexpr int kBucket = 4;
+
+__host__ __device__ __forceinline__ uint64_t hash_home(uint64_t hv, uint64_t mask) {
+    return (hv & mask) & ~(uint64_t)(kBucket - 1);
+}
+
+// Index stored for key (the first row holding it), or -1.
 template <int W>
 __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& key) {
     const uint64_t hv = key_hash<W>(key);
     const uint32_t fp = (uint32_t)(hv >> 32);
-    uint64_t i = hv & h.mask;
-    for (uint64_t probe = 0; probe <= h.mask; ++probe) {
-        const uint64_t s = __ldg(h.slots + i);
-        if (s == kEmptySlot) return -1;
-        if ((uint32_t)(s >> 32) == fp) {
-            const int64_t idx = (int64_t)(uint32_t)s;
-            if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
+    uint64_t b = hash_home(hv, h.mask);
+    for (uint64_t probe = 0; probe <= h.mask; probe += kBucket) {
+        const ulonglong2* bucket = reinterpret_cast<const ulonglong2*>(h.slots + b);
+        const ulonglong2 lo = __ldg(bucket), hi = __ldg(bucket + 1);
+        const uint64_t s[kBucket] = {lo.x, lo.y, hi.x, hi.y};
+        bool open = false;
+#pragma unroll
+        for (int k = 0; k < kBucket; ++k) {
+            if (s[k] == kEmptySlot) {
+                open = true;
+            } else if ((uint32_t)(s[k] >> 32) == fp) {
+                const int64_t idx = (int64_t)(uint32_t)s[k];
+                if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
+            }
         }
-        i = (i + 1) & h.mask;
+        if (open) return -1;
+        b = (b + kBucket) & h.mask;
     }
     return -1;
 }
@@ -721,6 +740,11 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
 
 // Grid for pivot_kernel: a few resident blocks per SM, looping over work items.
 int pivot_grid();
+
+// Which walk large term parts take: the grouped (warp per row) or the
+// pivot-major kernel.  QMBX_WALK=pivot or QMBX_WALK=grouped in the
+// environment overrides the default (grouped); read once per process.
+bool use_pivot_walk();
 
 // Grid for grouped_kernel: enough warps for every row, at most a few waves.
 int grouped_grid(int64_t n_rows);

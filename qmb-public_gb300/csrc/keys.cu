@@ -7,6 +7,8 @@
 // kernels on 64-bit key words.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "device.cuh"
 
 namespace qmbx {
@@ -365,7 +367,7 @@ __global__ void hash_insert_kernel(const uint64_t* __restrict__ keys, const int*
     Key<W> k = load_key<W>(keys, u);
     uint64_t hv = key_hash<W>(k);
     uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)u;
-    uint64_t i = hv & mask;
+    uint64_t i = hash_home(hv, mask);
     // the keys are unique and the table at most half full, so an empty slot
     // is reached within mask + 1 probes
     for (uint64_t probe = 0; probe <= mask; ++probe) {
@@ -391,7 +393,7 @@ RowSet take_rowset(Arena& ws, int64_t n) {
     out.head = ws.take<int32_t>(cap);
     out.pos = ws.take<int32_t>(cap);
     uint64_t slots = 64;
-    while (slots < 2 * cap) slots <<= 1;
+    while (slots < 4 * cap) slots <<= 1;
     out.slots = ws.take<uint64_t>(slots);
     out.slot_mask = slots - 1;
     out.sort = take_sort_scratch<W>(ws, n);
@@ -434,7 +436,7 @@ __global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_
     const Key<W> k = load_key<W>(keys, r);
     const uint64_t hv = key_hash<W>(k);
     const uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)r;
-    uint64_t i = hv & mask;
+    uint64_t i = hash_home(hv, mask);
     unsigned long long* sl = reinterpret_cast<unsigned long long*>(slots);
     for (uint64_t probe = 0; probe <= mask; ++probe) {
         unsigned long long cur = sl[i];
@@ -476,7 +478,7 @@ HashRows take_hashrows(Arena& ws, int64_t n) {
     out.n = n;
     out.keys = ws.take<uint64_t>(cap * W);
     uint64_t slots = 64;
-    while (slots < 2 * cap) slots <<= 1;
+    while (slots < 4 * cap) slots <<= 1;
     out.slots = ws.take<uint64_t>(slots);
     out.slot_mask = slots - 1;
     out.first = ws.take<int32_t>(cap);
@@ -541,6 +543,15 @@ static int sm_count() {
 }
 
 int pivot_grid() { return sm_count() * 4; }
+
+bool use_pivot_walk() {
+    static int mode = -1;
+    if (mode < 0) {
+        const char* e = getenv("QMBX_WALK");
+        mode = (e != nullptr && e[0] == 'p') ? 1 : 0;
+    }
+    return mode == 1;
+}
 
 int grouped_grid(int64_t n_rows) {
     static int sms[64] = {0};
