@@ -196,6 +196,23 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 
+def max_over_ranks(values: list[float], device=None) -> list[float]:
+    """Element-wise maximum of per-rank timings (the slowest rank sets the step time)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return list(values)
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def replica_value(units_per_rank: float, ms_per_step: float, world: int) -> float:
+    """Whole-job throughput of `world` replicas that each process units_per_rank per step."""
+    return world * units_per_rank / (ms_per_step * 1e-3)
+
+
 def measured_peaks() -> tuple[float, str]:
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -207,7 +224,7 @@ def measured_peaks() -> tuple[float, str]:
 
 def ncu_traffic(workload: str):
     """DRAM bytes per enumeration launch from the committed ncu summary, or None."""
-    path = os.path.join(REPO, "profiles", f"enumerate_kernel_{workload}.md")
+    path = os.path.join(REPO, "profiles", f"term_walk_{workload}.md")
     try:
         text = open(path).read()
     except OSError:
@@ -282,10 +299,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
 
     ms64 = timed(step64, args.steps)
 
-    if world > 1:
-        t = torch.tensor([ms32, ms64], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32, ms64 = float(t[0]), float(t[1])
+    ms32, ms64 = max_over_ranks([ms32, ms64], device)
 
     # find_relative (top K excluding configs_i)
     K = wl["spec"]["count_selected"]
@@ -337,7 +351,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     peak, peak_kind = measured_peaks()
     achieved = alg / (per_launch_ms * 1e-3) / 1e9
     ms_step32 = ms32 / args.steps
-    value = world * units / (ms_step32 * 1e-3)
+    value = replica_value(units, ms_step32, world)
     line = {
         "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
         "value": value,
@@ -355,7 +369,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
                    "n_qubytes": nq, "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MB write) before every timed step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ncu_traffic(args.workload), "kernel": "enumerate_kernel",
+                     "traffic": ncu_traffic(args.workload), "kernel": "term walk (grouped_kernel)",
                      "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_ms,
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "cpu_baseline": cpu,
