@@ -97,33 +97,38 @@ __device__ __forceinline__ bool key_eq(const Key<W>& a, const Key<W>& b) {
 
 constexpr uint64_t kEmptySlot = ~0ull;
 
+// Multiply mixing, one 64-bit multiply per key word; the high bits of the
+// result depend on every bit of the key and select the bucket.
 template <int W>
 __host__ __device__ __forceinline__ uint64_t key_hash(const Key<W>& k) {
-    uint64_t h = 0x9E3779B97F4A7C15ull;
-    for (int q = 0; q < W; ++q) {
-        h = (h ^ k.w[q]) * 0xBF58476D1CE4E5B9ull;
-        h ^= h >> 31;
-    }
-    h *= 0x94D049BB133111EBull;
-    h ^= h >> 29;
+    uint64_t h = k.w[0] * 0x9E3779B97F4A7C15ull;
+    for (int q = 1; q < W; ++q) h = (h ^ (h >> 31) ^ k.w[q]) * 0xBF58476D1CE4E5B9ull;
     return h;
 }
 
 struct HashView {
     const uint64_t* slots;
-    const uint64_t* keys;  // unique keys, n x W
+    const uint64_t* keys;  // keys of the set's rows, n x W
     uint64_t mask;         // slot count - 1 (a power of two minus one)
+    int shift;             // 64 - log2(slot count / kBucket)
 };
 
 // Probing runs over 4-slot buckets (32 bytes, one L2 sector): a key's home
-// is the bucket its hash selects, and a lookup loads a whole bucket with two
-// 16-byte loads; with the table at most a quarter full it almost always ends
-// in the home bucket.  Inserts fill the same sequence slot by slot, so a
-// bucket with an empty slot ends an unsuccessful search.
+// bucket is selected by the top bits of its hash, and a lookup loads a whole
+// bucket with two 16-byte loads; with the table at most a quarter full it
+// almost always ends in the home bucket.  Inserts fill the same sequence
+// slot by slot, so a bucket with an empty slot ends an unsuccessful search.
+// An entry is (hash high word << 32) | row; the high word is compared first.
 constexpr int kBucket = 4;
 
-__host__ __device__ __forceinline__ uint64_t hash_home(uint64_t hv, uint64_t mask) {
-    return (hv & mask) & ~(uint64_t)(kBucket - 1);
+__host__ __device__ __forceinline__ uint64_t hash_home(uint64_t hv, int shift) {
+    return (hv >> shift) * (uint64_t)kBucket;
+}
+
+__host__ __device__ __forceinline__ int hash_shift(uint64_t slots) {
+    int s = 64;
+    for (uint64_t b = slots / kBucket; b > 1; b >>= 1) --s;
+    return s;
 }
 
 // Index stored for key (the first row holding it), or -1.
@@ -131,19 +136,19 @@ template <int W>
 __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& key) {
     const uint64_t hv = key_hash<W>(key);
     const uint32_t fp = (uint32_t)(hv >> 32);
-    uint64_t b = hash_home(hv, h.mask);
+    uint64_t b = hash_home(hv, h.shift);
     for (uint64_t probe = 0; probe <= h.mask; probe += kBucket) {
-        const ulonglong2* bucket = reinterpret_cast<const ulonglong2*>(h.slots + b);
-        const ulonglong2 lo = __ldg(bucket), hi = __ldg(bucket + 1);
-        const uint64_t s[kBucket] = {lo.x, lo.y, hi.x, hi.y};
+        const uint4* bucket = reinterpret_cast<const uint4*>(h.slots + b);
+        const uint4 lo = __ldg(bucket), hi = __ldg(bucket + 1);
+        // (low, high) words of the four entries
+        const uint32_t idx[kBucket] = {lo.x, lo.z, hi.x, hi.z};
+        const uint32_t tag[kBucket] = {lo.y, lo.w, hi.y, hi.w};
         bool open = false;
 #pragma unroll
         for (int k = 0; k < kBucket; ++k) {
-            if (s[k] == kEmptySlot) {
-                open = true;
-            } else if ((uint32_t)(s[k] >> 32) == fp) {
-                const int64_t idx = (int64_t)(uint32_t)s[k];
-                if (key_eq<W>(load_key<W>(h.keys, idx), key)) return idx;
+            open |= idx[k] == 0xffffffffu;
+            if (tag[k] == fp && idx[k] != 0xffffffffu) {
+                if (key_eq<W>(load_key<W>(h.keys, (int64_t)idx[k]), key)) return (int64_t)idx[k];
             }
         }
         if (open) return -1;
@@ -416,8 +421,11 @@ __device__ __forceinline__ TermRec<W> load_term(const PartView& pv, int64_t t) {
 // (FP64 on GB300 issues at a small fraction of the FP32 rate) then runs with
 // all lanes active instead of once per divergent warp iteration.
 struct HitQueue {
-    int2* q;    // 64 entries: (slot | parity << 31, looked-up row)
-    int count;  // warp-uniform
+    int2* q;         // 64 entries: (slot | parity << 31, looked-up row)
+    int count;       // warp-uniform
+    uint64_t* ckey;  // 64 candidate images (W words each) waiting for their lookup
+    int* cmeta;      // slot | parity << 31 of each candidate
+    int ccount;      // warp-uniform
 };
 
 template <class V>
@@ -466,17 +474,71 @@ __device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, cons
     }
 }
 
-// Walk one group: lanes over its terms (warp-uniform bounds, so hits can be queued).
+// Look up the first n (<= 32) queued candidates, one per lane, queue the
+// hits, and move the remaining candidates to the front.
+template <int W, class V>
+__device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& acc, HitQueue& hq, int lane, int n) {
+    int2 h = make_int2(0, 0);
+    bool hit = false;
+    if (lane < n) {
+        const Key<W> img = load_key<W>(hq.ckey, lane);
+        const int64_t pos = hash_find<W>(v.lookup, img);
+        if (pos >= 0) {
+            hit = true;
+            h = make_int2(hq.cmeta[lane], (int)pos);
+        }
+    }
+    __syncwarp();
+    const int rest = hq.ccount - n;
+    if (lane < rest) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) hq.ckey[lane * W + q] = hq.ckey[(n + lane) * W + q];
+        hq.cmeta[lane] = hq.cmeta[n + lane];
+    }
+    __syncwarp();
+    hq.ccount = rest;
+    queue_push(v, acc, hq, lane, hit, h);
+}
+
+// Walk one group: lanes over its terms (warp-uniform bounds, so work can be
+// queued).  For batched visitors the applicable terms are first compacted
+// into the candidate queue, so that their lookups run with all lanes busy.
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& acc, const Key<W>& c,
                                                  const PartView& pv, int64_t g, int lane, HitQueue& hq) {
     const int2 se = __ldg(pv.groups + g);
-    for (int64_t base = se.x; base < se.y; base += 32) {
-        const int64_t t = base + lane;
-        int2 h = make_int2(0, 0);
-        bool hit = false;
-        if (t < se.y) hit = test_term<W, DIAG>(v, acc, c, pv, t, h);
-        if constexpr (V::kBatched && !DIAG) queue_push(v, acc, hq, lane, hit, h);
+    if constexpr (V::kBatched && !DIAG) {
+        const unsigned lt = (1u << lane) - 1u;
+        for (int base = se.x; base < se.y; base += 32) {
+            const int t = base + lane;
+            bool app = false;
+            Key<W> img;
+            int par = 0;
+            if (t < se.y) {
+                const TermRec<W> rec = load_term<W>(pv, t);
+                app = rec.applies(c);
+                if (app) par = rec.image(c, img);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, app);
+            if (m == 0) continue;
+            if (app) {
+                const int at = hq.ccount + __popc(m & lt);
+#pragma unroll
+                for (int q = 0; q < W; ++q) hq.ckey[at * W + q] = img.w[q];
+                hq.cmeta[at] = t | (par << 31);
+            }
+            hq.ccount += __popc(m);
+            __syncwarp();
+            if (hq.ccount >= 32) candidates_flush<W>(v, acc, hq, lane, 32);
+        }
+    } else {
+        for (int64_t base = se.x; base < se.y; base += 32) {
+            const int64_t t = base + lane;
+            int2 h = make_int2(0, 0);
+            bool hit = false;
+            if (t < se.y) hit = test_term<W, DIAG>(v, acc, c, pv, t, h);
+            if constexpr (V::kBatched && !DIAG) queue_push(v, acc, hq, lane, hit, h);
+        }
     }
 }
 
@@ -582,6 +644,8 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
                                                            int64_t n_max, PartView off, PartView diag) {
     __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
     __shared__ int2 hitq[kWarpsPerBlock][64];
+    __shared__ uint64_t candkey[V::kBatched ? kWarpsPerBlock : 1][64 * W];
+    __shared__ int candmeta[V::kBatched ? kWarpsPerBlock : 1][64];
     v.block_init(sh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -592,9 +656,12 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
         const Key<W> c = src.get(row);
         typename V::Acc acc;
         v.init(acc, row, c, sh);
-        HitQueue hq{hitq[warp], 0};
+        HitQueue hq{hitq[warp], 0, candkey[V::kBatched ? warp : 0], candmeta[V::kBatched ? warp : 0], 0};
         walk_part<W, false>(v, acc, c, off, lane, hq);
-        if constexpr (V::kBatched) queue_drain(v, acc, hq, lane, true);
+        if constexpr (V::kBatched) {
+            if (hq.ccount > 0) candidates_flush<W>(v, acc, hq, lane, hq.ccount);
+            queue_drain(v, acc, hq, lane, true);
+        }
         walk_part<W, true>(v, acc, c, diag, lane, hq);
         v.reduce(acc);
         if (lane == 0) v.finish(acc, row, c);
@@ -802,7 +869,7 @@ struct RowSet {
     uint64_t slot_mask;
     SortScratch sort;
     int64_t n;
-    HashView hash() const { return HashView{slots, keys, slot_mask}; }
+    HashView hash() const { return HashView{slots, keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>
@@ -827,7 +894,7 @@ struct HashRows {
     int* count;
     int32_t* scan;      // scan scratch
     int64_t n;
-    HashView hash() const { return HashView{slots, keys, slot_mask}; }
+    HashView hash() const { return HashView{slots, keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>

@@ -367,7 +367,7 @@ __global__ void hash_insert_kernel(const uint64_t* __restrict__ keys, const int*
     Key<W> k = load_key<W>(keys, u);
     uint64_t hv = key_hash<W>(k);
     uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)u;
-    uint64_t i = hash_home(hv, mask);
+    uint64_t i = hash_home(hv, hash_shift(mask + 1));
     // the keys are unique and the table at most half full, so an empty slot
     // is reached within mask + 1 probes
     for (uint64_t probe = 0; probe <= mask; ++probe) {
@@ -436,7 +436,7 @@ __global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_
     const Key<W> k = load_key<W>(keys, r);
     const uint64_t hv = key_hash<W>(k);
     const uint64_t entry = (hv & 0xffffffff00000000ull) | (uint64_t)(uint32_t)r;
-    uint64_t i = hash_home(hv, mask);
+    uint64_t i = hash_home(hv, hash_shift(mask + 1));
     unsigned long long* sl = reinterpret_cast<unsigned long long*>(slots);
     for (uint64_t probe = 0; probe <= mask; ++probe) {
         unsigned long long cur = sl[i];
