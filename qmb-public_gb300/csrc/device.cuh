@@ -481,7 +481,9 @@ __device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& ac
     int2 h = make_int2(0, 0);
     bool hit = false;
     if (lane < n) {
-        const Key<W> img = load_key<W>(hq.ckey, lane);
+        Key<W> img;  // plain loads: the candidate queue is in shared memory
+#pragma unroll
+        for (int q = 0; q < W; ++q) img.w[q] = hq.ckey[lane * W + q];
         const int64_t pos = hash_find<W>(v.lookup, img);
         if (pos >= 0) {
             hit = true;
