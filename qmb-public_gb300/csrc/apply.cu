@@ -536,6 +536,18 @@ int launch_walk(const V& v, const HashRows& walk, const PartView& part, const Pa
     return QMBX_OK;
 }
 
+// Tiled pass over the diagonal terms of every walked row (adds into res).
+template <int W, class D>
+int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
+    if (diag.n == 0) return QMBX_OK;
+    UniqueRows<W> src{walk.keys, walk.unique};
+    PartView none = part;
+    none.n = 0;
+    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+    QMBX_LAUNCH_CHECK("apply_within diagonal pass");
+    return QMBX_OK;
+}
+
 // Pivot-major walk of the changing terms (results added into res by the
 // visitor's flush or hits) followed by a tiled pass over the diagonal terms.
 template <int W, class V, class D>
@@ -544,13 +556,7 @@ int launch_pivot(const V& v, const D& dv, const HashRows& walk, const PartView& 
     UniqueRows<W> src{walk.keys, walk.unique};
     QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, walk.count, walk.n, part));
     QMBX_LAUNCH_CHECK("apply_within pivot walk");
-    if (diag.n > 0) {
-        PartView none = part;
-        none.n = 0;
-        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
-        QMBX_LAUNCH_CHECK("apply_within diagonal pass");
-    }
-    return QMBX_OK;
+    return launch_diag<W>(dv, walk, part, diag, s);
 }
 
 // Forward maps amplitudes on configs_i (input side) to configs_j (output
@@ -617,6 +623,11 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashRows& walk = scatter ? in_set : out_set;
     const HashView look = scatter ? out_set.hash() : in_set.hash();
+    // large parts without the pivot walk: the grouped kernel walks the
+    // changing terms and a tiled pass adds the diagonal ones
+    const bool grouped = !pivot && part.n >= kGroupedMinTerms;
+    PartView walk_diag = diag;
+    if (grouped) walk_diag.n = 0;
     if (pivot) {
 #define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
     {                                                                                                            \
@@ -643,40 +654,63 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
                 Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
                 Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         } else {
             if (a.adjoint) {
                 Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
                 Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
     } else {
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
                 GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
                 GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         } else {
             if (a.adjoint) {
                 GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
                 GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
-                st = launch_walk<W>(v, walk, part, diag, s);
+                st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
     }
     if (st != QMBX_OK) return st;
+    if (grouped && diag.n > 0) {
+        const bool f32 = a.prec == Prec::F32C;
+#define QMBX_DIAG_CASE(CONJ, F32, SCATTER)                                              \
+    {                                                                                   \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, res};  \
+        st = launch_diag<W>(dv, walk, part, diag, s);                                   \
+    }
+        if (scatter) {
+            if (a.adjoint) {
+                if (f32) QMBX_DIAG_CASE(true, true, true) else QMBX_DIAG_CASE(true, false, true)
+            } else {
+                if (f32) QMBX_DIAG_CASE(false, true, true) else QMBX_DIAG_CASE(false, false, true)
+            }
+        } else {
+            if (a.adjoint) {
+                if (f32) QMBX_DIAG_CASE(true, true, false) else QMBX_DIAG_CASE(true, false, false)
+            } else {
+                if (f32) QMBX_DIAG_CASE(false, true, false) else QMBX_DIAG_CASE(false, false, false)
+            }
+        }
+#undef QMBX_DIAG_CASE
+        if (st != QMBX_OK) return st;
+    }
     QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_out, kThreads), kThreads, 0, s>>>(res, out_set.first, n_out, a.adjoint ? 1 : 0, a.out64, a.out32));
     QMBX_LAUNCH_CHECK("apply_finalize_kernel");
     return QMBX_OK;

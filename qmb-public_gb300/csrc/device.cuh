@@ -511,27 +511,32 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
     const int2 se = __ldg(pv.groups + g);
     if constexpr (V::kBatched && !DIAG) {
         const unsigned lt = (1u << lane) - 1u;
-        for (int base = se.x; base < se.y; base += 32) {
-            const int t = base + lane;
-            bool app = false;
-            Key<W> img;
-            int par = 0;
-            if (t < se.y) {
-                const TermRec<W> rec = load_term<W>(pv, t);
-                app = rec.applies(c);
-                if (app) par = rec.image(c, img);
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, app);
-            if (m == 0) continue;
-            if (app) {
-                const int at = hq.ccount + __popc(m & lt);
+        // two terms per lane per step: both records are loaded before either is tested
+        for (int base = se.x; base < se.y; base += 64) {
+            const int t0 = base + lane, t1 = base + 32 + lane;
+            TermRec<W> r0, r1;
+            const bool in0 = t0 < se.y, in1 = t1 < se.y;
+            if (in0) r0 = load_term<W>(pv, t0);
+            if (in1) r1 = load_term<W>(pv, t1);
 #pragma unroll
-                for (int q = 0; q < W; ++q) hq.ckey[at * W + q] = img.w[q];
-                hq.cmeta[at] = t | (par << 31);
+            for (int half = 0; half < 2; ++half) {
+                const TermRec<W>& rec = half ? r1 : r0;
+                const int t = half ? t1 : t0;
+                const bool app = (half ? in1 : in0) && rec.applies(c);
+                const unsigned m = __ballot_sync(0xffffffffu, app);
+                if (m == 0) continue;
+                if (app) {
+                    Key<W> img;
+                    const int par = rec.image(c, img);
+                    const int at = hq.ccount + __popc(m & lt);
+#pragma unroll
+                    for (int q = 0; q < W; ++q) hq.ckey[at * W + q] = img.w[q];
+                    hq.cmeta[at] = t | (par << 31);
+                }
+                hq.ccount += __popc(m);
+                __syncwarp();
+                if (hq.ccount >= 32) candidates_flush<W>(v, acc, hq, lane, 32);
             }
-            hq.ccount += __popc(m);
-            __syncwarp();
-            if (hq.ccount >= 32) candidates_flush<W>(v, acc, hq, lane, 32);
         }
     } else {
         for (int64_t base = se.x; base < se.y; base += 32) {
