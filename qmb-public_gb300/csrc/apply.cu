@@ -619,7 +619,7 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     // (gather) with daggered terms for the forward map or forward terms
     // (conjugated) for the adjoint
     const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
-    const bool pivot = part.n >= kGroupedMinTerms && use_pivot_walk();
+    const bool pivot = part.n >= kGroupedMinTerms && use_pivot_walk(part);
     if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashRows& walk = scatter ? in_set : out_set;
     const HashView look = scatter ? out_set.hash() : in_set.hash();

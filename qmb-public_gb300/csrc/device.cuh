@@ -815,10 +815,12 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
 // Grid for pivot_kernel: a few resident blocks per SM, looping over work items.
 int pivot_grid();
 
-// Which walk large term parts take: the grouped (warp per row) or the
-// pivot-major kernel.  QMBX_WALK=pivot or QMBX_WALK=grouped in the
-// environment overrides the default (grouped); read once per process.
-bool use_pivot_walk();
+// Which walk a large term part takes: the pivot-major kernel when its
+// non-empty groups hold kPivotMeanGroup terms or more on average, the
+// grouped (warp per row) kernel otherwise.  QMBX_WALK=pivot or
+// QMBX_WALK=grouped in the environment forces one; read once per process.
+constexpr int kPivotMeanGroup = 768;
+bool use_pivot_walk(const PartView& part);
 
 // Grid for grouped_kernel: enough warps for every row, at most a few waves.
 int grouped_grid(int64_t n_rows);

@@ -544,13 +544,15 @@ static int sm_count() {
 
 int pivot_grid() { return sm_count() * 4; }
 
-bool use_pivot_walk() {
-    static int mode = -1;
-    if (mode < 0) {
+bool use_pivot_walk(const PartView& part) {
+    static int mode = -2;  // -1 automatic, 0 grouped, 1 pivot
+    if (mode == -2) {
         const char* e = getenv("QMBX_WALK");
-        mode = (e != nullptr && e[0] == 'p') ? 1 : 0;
+        mode = (e != nullptr && e[0] == 'p') ? 1 : (e != nullptr && e[0] == 'g') ? 0 : -1;
     }
-    return mode == 1;
+    if (mode >= 0) return mode == 1;
+    // groups holding hundreds of terms amortise staging them in shared memory
+    return part.n_nonempty > 0 && part.n >= (int64_t)kPivotMeanGroup * part.n_nonempty;
 }
 
 int grouped_grid(int64_t n_rows) {

@@ -138,7 +138,7 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
     v.a = r;
     v.lookup = r.excl;
     KeyRows<W> src{keys_i};
-    if (r.off.n >= kGroupedMinTerms && !use_pivot_walk()) {
+    if (r.off.n >= kGroupedMinTerms && !use_pivot_walk(r.off)) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
     } else if (r.off.n >= kGroupedMinTerms) {
         // pivot-major walk of the changing terms, then the diagonal terms tiled

@@ -96,15 +96,20 @@ def random_integrals(n_orbit: int, seed: int, *, complex_valued: bool = False):
 
 
 def integral_terms(n_orbit: int, seed: int, *, complex_valued: bool = False):
-    """Normal-ordered fermion terms of the synthetic integrals.
-
-    Returns ``(keys, coefs)``: ``keys`` int16[T, 4] spin-orbital indices of
-    a+_P a+_Q a_R a_S (one-body rows use slots 0-1, the constant row none) and
-    ``ops`` int8 count per row, in a deterministic order (constant, one-body,
-    two-body by key); ``coefs`` complex128[T].
-    """
+    """Normal-ordered fermion terms of the seeded synthetic integrals (see ``terms_from_integrals``)."""
     e0, h, eri = random_integrals(n_orbit, seed, complex_valued=complex_valued)
-    n = n_orbit
+    return terms_from_integrals(e0, h, eri)
+
+
+def terms_from_integrals(e0: float, h: np.ndarray, eri: np.ndarray):
+    """Normal-ordered fermion terms of the integrals (e0, h[p,q], chemist (pq|rs)).
+
+    Returns numpy ``(site, kind, coef)`` in a deterministic order: the
+    constant, the one-body terms a+_P a_Q by (P, Q), the two-body terms
+    a+_P a+_Q a_R a_S (P > Q, R > S) by key; spin orbitals interleaved
+    (alpha 2p, beta 2p + 1).
+    """
+    n = h.shape[0]
     ns = 2 * n
     # one-body: a+_P a_Q, same spin
     p, q = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
@@ -196,6 +201,80 @@ def integral_hamiltonian_tables(n_orbit: int, seed: int, *, complex_valued: bool
     """``(site, kind, coef)`` torch tensors ordered as ``Hamiltonian(dict)`` orders them."""
     site, kind, coef = integral_terms(n_orbit, seed, complex_valued=complex_valued)
     return sort_terms(torch.from_numpy(site), torch.from_numpy(kind), torch.from_numpy(coef))
+
+
+def read_fcidump(path: str):
+    """Read an FCIDUMP file (optionally gzip-compressed) into a term table.
+
+    Restates the parsing of qmb/fcidump.py:50-95: the header's NORB, NELEC and
+    MS2; integral lines ``value i j k l`` with 1-based orbitals, where
+    (0,0,0,0) is the constant, (i,0,0,0) is skipped, (i,j,0,0) a symmetric
+    one-body integral, (i,j,k,l) a chemist two-body integral (ij|kl) with its
+    8-fold permutations, (i,j,k,0) an error.  The integrals then become
+    normal-ordered terms as in ``terms_from_integrals`` (no openfermion
+    needed) and are ordered as ``Hamiltonian(dict)`` orders them.
+    Returns ``(n_orbit, n_electron, ms2, site, kind, coef)`` with torch tensors.
+    """
+    import gzip
+    import re
+
+    opener = gzip.open if str(path).endswith(".gz") else open
+    with opener(path, "rt", encoding="utf-8") as f:
+        n_orbit = n_electron = ms2 = None
+        for line in f:
+            low = line.lower()
+            if (m := re.search(r"norb\s*=\s*(\d+)", low)) is not None:
+                n_orbit = int(m.group(1))
+            if (m := re.search(r"nelec\s*=\s*(\d+)", low)) is not None:
+                n_electron = int(m.group(1))
+            if (m := re.search(r"ms2\s*=\s*(\d+)", low)) is not None:
+                ms2 = int(m.group(1))
+            if "&end" in low or "/" == low.strip():
+                break
+        if n_orbit is None or n_electron is None or ms2 is None:
+            raise ValueError("FCIDUMP header lacks NORB, NELEC or MS2")
+        e0 = 0.0
+        h = np.zeros((n_orbit, n_orbit))
+        eri = np.zeros((n_orbit,) * 4)
+        for line in f:
+            parts = line.split()
+            if not parts:
+                continue
+            value = float(parts[0].replace("D", "E").replace("d", "e"))
+            i, j, k, l = (int(x) - 1 for x in parts[1:5])
+            if (i, j, k, l) == (-1, -1, -1, -1):
+                e0 = value
+            elif j == -1 and k == -1 and l == -1:
+                continue
+            elif k == -1 and l == -1:
+                h[i, j] = h[j, i] = value
+            elif l == -1:
+                raise ValueError(f"invalid FCIDUMP line: {line.strip()}")
+            else:
+                for a, b, c, d in ((i, j, k, l), (i, j, l, k), (j, i, k, l), (j, i, l, k), (l, k, j, i), (k, l, j, i),
+                                   (l, k, i, j), (k, l, i, j)):
+                    eri[a, b, c, d] = value
+    site, kind, coef = terms_from_integrals(e0, h, eri)
+    site, kind, coef = sort_terms(torch.from_numpy(site), torch.from_numpy(kind), torch.from_numpy(coef))
+    return n_orbit, n_electron, ms2, site, kind, coef
+
+
+def write_fcidump(path: str, e0: float, h: np.ndarray, eri: np.ndarray, n_electron: int, ms2: int = 0) -> None:
+    """Write real integrals in FCIDUMP form (unique 8-fold two-body entries, i >= j, k >= l, ij >= kl)."""
+    n = h.shape[0]
+    with open(path, "w", encoding="utf-8") as f:
+        f.write(f" &FCI NORB={n},NELEC={n_electron},MS2={ms2},\n  ORBSYM={','.join(['1'] * n)},\n  ISYM=1,\n &END\n")
+        for i in range(n):
+            for j in range(i + 1):
+                for k in range(n):
+                    for l in range(k + 1):
+                        if i * (i + 1) // 2 + j >= k * (k + 1) // 2 + l and eri[i, j, k, l] != 0.0:
+                            f.write(f"{eri[i, j, k, l]:.17e} {i + 1} {j + 1} {k + 1} {l + 1}\n")
+        for i in range(n):
+            for j in range(i + 1):
+                if h[i, j] != 0.0:
+                    f.write(f"{h[i, j]:.17e} {i + 1} {j + 1} 0 0\n")
+        f.write(f"{e0:.17e} 0 0 0 0\n")
 
 
 def n_integral_terms(n_orbit: int) -> int:

@@ -76,3 +76,32 @@ def test_hubbard_term_count():
     assert len(d) == 64 + 4 * 112
     site, kind, coef = terms.prepare(d)
     assert site.dtype == torch.int16 and kind.dtype == torch.uint8 and coef.dtype == torch.float64
+
+
+def test_fcidump_round_trip(tmp_path):
+    e0, h, eri = terms.random_integrals(5, seed=9)
+    path = tmp_path / "toy.FCIDUMP"
+    terms.write_fcidump(str(path), e0, h, eri, n_electron=6)
+    n_orbit, n_electron, ms2, site, kind, coef = terms.read_fcidump(str(path))
+    assert (n_orbit, n_electron, ms2) == (5, 6, 0)
+    ref = terms.sort_terms(*(torch.from_numpy(x) for x in terms.terms_from_integrals(e0, h, eri)))
+    assert torch.equal(kind, ref[1])
+    live = ref[1] != 2
+    assert torch.equal(site[live], ref[0][live])
+    torch.testing.assert_close(coef, ref[2], rtol=1e-15, atol=1e-15)
+
+
+def test_fcidump_gzip_and_bad_line(tmp_path):
+    import gzip
+
+    e0, h, eri = terms.random_integrals(3, seed=4)
+    plain = tmp_path / "a.FCIDUMP"
+    terms.write_fcidump(str(plain), e0, h, eri, n_electron=2)
+    gz = tmp_path / "a.FCIDUMP.gz"
+    with open(plain, "rb") as src, gzip.open(gz, "wb") as dst:
+        dst.write(src.read())
+    assert terms.read_fcidump(str(gz))[0] == 3
+    bad = tmp_path / "bad.FCIDUMP"
+    bad.write_text(" &FCI NORB=2,NELEC=2,MS2=0,\n &END\n 1.0 1 2 1 0\n")
+    with pytest.raises(ValueError):
+        terms.read_fcidump(str(bad))
