@@ -52,6 +52,13 @@ WORKLOADS = {
                description="ab-initio 28 spin orbitals (n_qubytes 4), 5a+5b, N_i 20000, N_j 200000, K 50000"),
     "c1": dict(n_orbit=6, n_alpha=3, n_beta=3, n_i=400, n_j=400, count_selected=100, seed=2024,
                description="ab-initio 12 spin orbitals (n_qubytes 2), 3a+3b, all 400 determinants"),
+    "lanczos": dict(n_orbit=26, n_alpha=7, n_beta=7, n_i=65536, n_j=65536, count_selected=0, seed=2025,
+                    lanczos_steps=20,
+                    description="ab-initio 52 spin orbitals (n_qubytes 7), 7a+7b, 65536-determinant basis, "
+                                "20 Lanczos iterations"),
+    "pt2": dict(n_orbit=38, n_alpha=10, n_beta=10, n_i=8192, n_j=8192, count_selected=1000000, seed=2027,
+                description="ab-initio 76 spin orbitals (n_qubytes 10), 10a+10b, 8192 variational determinants, "
+                            "Epstein-Nesbet PT2 over the top 1,000,000 connection records"),
 }
 
 
@@ -436,7 +443,8 @@ def _timed_loop(fn, steps, device, flush=None):
 
 
 def run_extra(args, wl) -> dict:
-    """The other benchmark shapes: c3 (energy + gradient through an MLP), c4 (Hubbard 1M), c5 (find_relative 1M)."""
+    """The other benchmark shapes: c3 (energy + gradient through an MLP), c4 (Hubbard 1M), c5 (find_relative 1M),
+    and the engine's callers: lanczos (20 iterations on the c3 basis) and pt2 (one PT2 step on the c5 shape)."""
     import torch
 
     qmb = importlib.import_module("qmb-public_gb300")
@@ -498,6 +506,48 @@ def run_extra(args, wl) -> dict:
                      "value": 2 * T * n / (ms32 * 1e-3), "unit": "term-applications/s", "higher_is_better": True,
                      "ms_per_step": ms32, "fp64_ms_per_step": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
                      "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64)})
+    elif args.workload == "lanczos":
+        n_steps = wl["spec"]["lanczos_steps"]
+        gen = torch.Generator(device=device).manual_seed(wl["spec"]["seed"])
+        start = torch.randn([n], dtype=torch.complex128, device=device, generator=gen)
+        for _ in range(args.warmup):
+            qmb.lanczos_energy(ham, ci, 2, start=start)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            energy, _vec = qmb.lanczos_energy(ham, ci, n_steps, start=start)
+        torch.cuda.synchronize(device)
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        native.profile_enable(True)
+        qmb.lanczos_energy(ham, ci, n_steps, start=start)
+        torch.cuda.synchronize(device)
+        prof = native.profile_read()
+        native.profile_enable(False)
+        n_apply = n_steps + 2
+        line.update({"metric": "Lanczos wall time (20 iterations, FP64, Ritz value on the host)", "value": ms,
+                     "unit": "ms", "higher_is_better": False, "ms_per_iteration": ms / n_apply,
+                     "energy": energy, "apply_within_calls": n_apply,
+                     "term_applications_per_s": n_apply * T * n / (ms * 1e-3),
+                     "kernel_groups_ms_per_run": {g: prof["groups"][g][1] for g in prof["groups"]}})
+    elif args.workload == "pt2":
+        psi = torch.from_numpy(wl["psi"]).to(device)
+        K = wl["spec"]["count_selected"]
+        for _ in range(args.warmup):
+            qmb.pt2_energy(ham, ci, psi, K)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e0, e2 = qmb.pt2_energy(ham, ci, psi, K)
+        torch.cuda.synchronize(device)
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        native.profile_enable(True)
+        qmb.pt2_energy(ham, ci, psi, K)
+        torch.cuda.synchronize(device)
+        prof = native.profile_read()
+        native.profile_enable(False)
+        line.update({"metric": "PT2 step wall time (E0, find_relative, H psi on the selected rows, denominators)",
+                     "value": ms, "unit": "ms", "higher_is_better": False, "count_selected": K, "e0": e0, "e2": e2,
+                     "kernel_groups_ms_per_run": {g: prof["groups"][g][1] for g in prof["groups"]}})
     else:
         psi = torch.from_numpy(wl["psi"]).to(device)
         K = wl["spec"]["count_selected"]
@@ -561,7 +611,7 @@ def main():
 
     import torch
 
-    if args.workload in ("c3", "c4", "c5"):
+    if args.workload in ("c3", "c4", "c5", "lanczos", "pt2"):
         if rank == 0:
             print(json.dumps(run_extra(args, make_workload(args.workload))), flush=True)
         return

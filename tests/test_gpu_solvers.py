@@ -65,6 +65,29 @@ def test_pt2_matches_dense_epstein_nesbet(complex_valued, cuda_device):
 
     c = torch.from_numpy(rows[chosen]).to(cuda_device)
     psi = torch.from_numpy(psi0).to(cuda_device)
-    got0, got2 = pt2_energy(ham, c, psi, count_selected=rows.shape[0])
+    # count_selected caps connection records (one per term and source row), not rows: take them all
+    got0, got2 = pt2_energy(ham, c, psi, count_selected=100000)
+    assert abs(got0 - e0) <= 1e-12 * abs(e0)
+    assert abs(got2 - e2) <= 1e-10 * abs(e2)
+
+
+def test_pt2_with_a_capped_selection(cuda_device):
+    ham, rows, h = _system(True)
+    rng = np.random.default_rng(9)
+    chosen = np.sort(rng.choice(rows.shape[0], size=60, replace=False))
+    psi0 = rng.standard_normal(60) + 1j * rng.standard_normal(60)
+    c = torch.from_numpy(rows[chosen]).to(cuda_device)
+    psi = torch.from_numpy(psi0).to(cuda_device)
+    other = ham.find_relative(c, psi, 500, c).cpu().numpy()
+    assert 0 < other.shape[0] < rows.shape[0] - 60
+    index = {r.tobytes(): k for k, r in enumerate(rows)}
+    pick = np.array([index[r.tobytes()] for r in other])
+    full = np.zeros(rows.shape[0], dtype=np.complex128)
+    full[chosen] = psi0
+    norm = np.vdot(psi0, psi0).real
+    e0 = np.vdot(full, h @ full).real / norm
+    hpsi = h @ full
+    e2 = np.sum(np.abs(hpsi[pick]) ** 2 / norm / (e0 - np.diag(h).real[pick]))
+    got0, got2 = pt2_energy(ham, c, psi, count_selected=500)
     assert abs(got0 - e0) <= 1e-12 * abs(e0)
     assert abs(got2 - e2) <= 1e-10 * abs(e2)
