@@ -192,12 +192,13 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
 /* ---------------------------------------------------------------------------
  * Tracing (no counterpart in the reference, which has none).
  * Every kernel launch of this library increments a process-wide counter.
- * qmbx_profile_enable(1) additionally brackets the launches of four groups
- * (0 term enumeration, 1 key packing/sorting, 2 selection, 3 other) with
+ * qmbx_profile_enable(1) additionally brackets the launches of five groups
+ * (0 term walk, 1 key packing/sorting/hashing, 2 selection, 3 other,
+ * 4 the separate passes over diagonal terms) with
  * CUDA events on the launching stream and resets the totals;
  * qmbx_profile_read waits for the recorded events and returns the launch
  * counter and, per group, the number of timed launches and their total
- * milliseconds (arrays of 4).
+ * milliseconds (arrays of 5).
  * ------------------------------------------------------------------------- */
 
 int qmbx_profile_enable(int32_t on);

@@ -50,7 +50,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_profile_read": (ctypes.c_int, [_PI64, _PI64, ctypes.POINTER(ctypes.c_double)]),
 }
 
-PROFILE_GROUPS = ("enumerate", "keys", "select", "other")
+PROFILE_GROUPS = ("enumerate", "keys", "select", "other", "diagonal")
 
 
 def profile_enable(on: bool) -> None:
@@ -61,8 +61,8 @@ def profile_enable(on: bool) -> None:
 def profile_read() -> dict:
     """Launch counter and per-group (count, milliseconds) since the last profile_enable."""
     launches = ctypes.c_int64()
-    counts = (ctypes.c_int64 * 4)()
-    ms = (ctypes.c_double * 4)()
+    counts = (ctypes.c_int64 * len(PROFILE_GROUPS))()
+    ms = (ctypes.c_double * len(PROFILE_GROUPS))()
     check(library().qmbx_profile_read(ctypes.byref(launches), counts, ms))
     return {"launches": launches.value,
             "groups": {g: (counts[k], ms[k]) for k, g in enumerate(PROFILE_GROUPS)}}

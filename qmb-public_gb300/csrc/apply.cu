@@ -543,7 +543,7 @@ int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const P
     UniqueRows<W> src{walk.keys, walk.unique};
     PartView none = part;
     none.n = 0;
-    QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+    QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
     QMBX_LAUNCH_CHECK("apply_within diagonal pass");
     return QMBX_OK;
 }

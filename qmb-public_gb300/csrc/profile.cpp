@@ -27,8 +27,8 @@ struct Pending {
 };
 std::vector<Pending> g_pending;
 std::vector<cudaEvent_t> g_pool;
-int64_t g_count[kProfileGroups] = {0, 0, 0, 0};
-double g_ms[kProfileGroups] = {0, 0, 0, 0};
+int64_t g_count[kProfileGroups] = {};
+double g_ms[kProfileGroups] = {};
 
 cudaEvent_t take_event() {
     std::lock_guard<std::mutex> lock(g_mu);

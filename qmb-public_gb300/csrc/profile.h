@@ -5,7 +5,16 @@
 
 namespace qmbx {
 
-enum ProfileGroup { kGroupEnumerate = 0, kGroupKeys = 1, kGroupSelect = 2, kGroupOther = 3, kProfileGroups = 4 };
+// kGroupEnumerate is the main term walk; kGroupDiagonal the separate
+// passes over diagonal terms that follow it
+enum ProfileGroup {
+    kGroupEnumerate = 0,
+    kGroupKeys = 1,
+    kGroupSelect = 2,
+    kGroupOther = 3,
+    kGroupDiagonal = 4,
+    kProfileGroups = 5
+};
 
 void note_launch(int n);
 
