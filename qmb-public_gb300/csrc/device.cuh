@@ -89,13 +89,17 @@ __device__ __forceinline__ bool key_eq(const Key<W>& a, const Key<W>& b) {
 }
 
 // ---------------------------------------------------------------------------
-// open-addressing hash set over the unique keys of a row set
+// open-addressing hash set over the keys of a row set
 //
-// slot = (32-bit fingerprint << 32) | index of the key among the unique keys,
-// all ones when empty; linear probing, load factor at most 1/2.
+// Two parallel slot arrays: tags[i] is a 32-bit fingerprint of the key in
+// slot i (never all ones) and rows[i] the row holding it; both are all ones
+// when the slot is empty.  A lookup reads a bucket of four tags (16 bytes,
+// one L1 wavefront per lane) and touches rows[] and the key only on a tag
+// match, so an unsuccessful lookup costs one load.  Load factor <= 1/4.
 // ---------------------------------------------------------------------------
 
-constexpr uint64_t kEmptySlot = ~0ull;
+constexpr uint32_t kEmptyTag = 0xffffffffu;
+constexpr uint32_t kEmptyRow = 0xffffffffu;
 
 // Multiply mixing, one 64-bit multiply per key word; the high bits of the
 // result depend on every bit of the key and select the bucket.
@@ -107,19 +111,25 @@ __host__ __device__ __forceinline__ uint64_t key_hash(const Key<W>& k) {
 }
 
 struct HashView {
-    const uint64_t* slots;
+    const uint32_t* tags;  // slot count
+    const uint32_t* rows;  // slot count
     const uint64_t* keys;  // keys of the set's rows, n x W
     uint64_t mask;         // slot count - 1 (a power of two minus one)
     int shift;             // 64 - log2(slot count / kBucket)
 };
 
-// Probing runs over 4-slot buckets (32 bytes, one L2 sector): a key's home
-// bucket is selected by the top bits of its hash, and a lookup loads a whole
-// bucket with two 16-byte loads; with the table at most a quarter full it
-// almost always ends in the home bucket.  Inserts fill the same sequence
-// slot by slot, so a bucket with an empty slot ends an unsuccessful search.
-// An entry is (hash high word << 32) | row; the high word is compared first.
+// Probing runs over 4-slot buckets: a key's home bucket is selected by the
+// top bits of its hash, and a lookup loads the bucket's four tags with one
+// 16-byte load; with the table at most a quarter full it almost always ends
+// in the home bucket.  Inserts fill the same sequence slot by slot, so a
+// bucket with an empty slot ends an unsuccessful search.
 constexpr int kBucket = 4;
+
+// Fingerprint stored in tags[]: the hash's high word, kept off the empty value.
+__host__ __device__ __forceinline__ uint32_t hash_tag(uint64_t hv) {
+    const uint32_t t = (uint32_t)(hv >> 32);
+    return t == kEmptyTag ? kEmptyTag - 1u : t;
+}
 
 __host__ __device__ __forceinline__ uint64_t hash_home(uint64_t hv, int shift) {
     return (hv >> shift) * (uint64_t)kBucket;
@@ -131,24 +141,22 @@ __host__ __device__ __forceinline__ int hash_shift(uint64_t slots) {
     return s;
 }
 
-// Index stored for key (the first row holding it), or -1.
+// Row stored for key (the first row holding it), or -1.
 template <int W>
 __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& key) {
     const uint64_t hv = key_hash<W>(key);
-    const uint32_t fp = (uint32_t)(hv >> 32);
+    const uint32_t fp = hash_tag(hv);
     uint64_t b = hash_home(hv, h.shift);
     for (uint64_t probe = 0; probe <= h.mask; probe += kBucket) {
-        const uint4* bucket = reinterpret_cast<const uint4*>(h.slots + b);
-        const uint4 lo = __ldg(bucket), hi = __ldg(bucket + 1);
-        // (low, high) words of the four entries
-        const uint32_t idx[kBucket] = {lo.x, lo.z, hi.x, hi.z};
-        const uint32_t tag[kBucket] = {lo.y, lo.w, hi.y, hi.w};
+        const uint4 t4 = __ldg(reinterpret_cast<const uint4*>(h.tags + b));
+        const uint32_t tag[kBucket] = {t4.x, t4.y, t4.z, t4.w};
         bool open = false;
 #pragma unroll
         for (int k = 0; k < kBucket; ++k) {
-            open |= idx[k] == 0xffffffffu;
-            if (tag[k] == fp && idx[k] != 0xffffffffu) {
-                if (key_eq<W>(load_key<W>(h.keys, (int64_t)idx[k]), key)) return (int64_t)idx[k];
+            open |= tag[k] == kEmptyTag;
+            if (tag[k] == fp) {
+                const uint32_t row = __ldg(h.rows + b + k);
+                if (row != kEmptyRow && key_eq<W>(load_key<W>(h.keys, (int64_t)row), key)) return (int64_t)row;
             }
         }
         if (open) return -1;
@@ -162,7 +170,9 @@ __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& ke
 // ---------------------------------------------------------------------------
 
 struct PartView {
-    const uint64_t* term;   // [n][W][4] mask, val, flip, par
+    const ulonglong2* test;    // [W][stride]: (mask, val) per word
+    const ulonglong2* apply;   // [W][stride]: (flip, par) per word
+    int64_t stride;            // terms in the part (n may be set to 0 to skip a part)
     const double2* coef;
     const float4* coef32;
     const int32_t* orig;
@@ -181,7 +191,9 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
     const qmbx_table_part& p = h->part[which];
     const char* base = static_cast<const char*>(table_dev);
     PartView v;
-    v.term = reinterpret_cast<const uint64_t*>(base + p.off_term);
+    v.test = reinterpret_cast<const ulonglong2*>(base + p.off_test);
+    v.apply = reinterpret_cast<const ulonglong2*>(base + p.off_apply);
+    v.stride = p.n;
     v.coef = reinterpret_cast<const double2*>(base + p.off_coef);
     v.coef32 = reinterpret_cast<const float4*>(base + p.off_coef32);
     v.orig = reinterpret_cast<const int32_t*>(base + p.off_orig);
@@ -207,17 +219,30 @@ int check_table(const void* table_host, const void* table_dev);
 constexpr int kTermTile = 128;
 
 template <int W>
-struct TermTile {
+struct __align__(16) TermTile {
     uint64_t m[kTermTile][4 * W];  // per word: mask, val, flip, par
 };
 
+// Copy count terms from t0 into records of 4W words (per word mask, val,
+// flip, par) at dst, threads striding over terms one word at a time.
+template <int W>
+__device__ __forceinline__ void stage_terms(uint64_t* dst, const PartView& part, int64_t t0, int count, int tid,
+                                            int nthreads) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        const ulonglong2* test = part.test + (int64_t)q * part.stride + t0;
+        const ulonglong2* apply = part.apply + (int64_t)q * part.stride + t0;
+        for (int k = tid; k < count; k += nthreads) {
+            ulonglong2* rec = reinterpret_cast<ulonglong2*>(dst + (int64_t)k * 4 * W + 4 * q);
+            rec[0] = __ldg(test + k);
+            rec[1] = __ldg(apply + k);
+        }
+    }
+}
+
 template <int W>
 __device__ __forceinline__ void stage_tile(TermTile<W>& tile, const PartView& part, int64_t t0, int count) {
-    // 4W words per term, copied as 16-byte pairs
-    const int total = count * 2 * W;
-    const ulonglong2* src = reinterpret_cast<const ulonglong2*>(part.term + t0 * 4 * W);
-    ulonglong2* dst = reinterpret_cast<ulonglong2*>(&tile.m[0][0]);
-    for (int k = threadIdx.x; k < total; k += blockDim.x) dst[k] = __ldg(src + k);
+    stage_terms<W>(&tile.m[0][0], part, t0, count, threadIdx.x, blockDim.x);
 }
 
 template <int W>
@@ -403,17 +428,26 @@ struct TermRec {
     }
 };
 
+// The test pair of every word of term t (into m[4q], m[4q + 1]).
 template <int W>
-__device__ __forceinline__ TermRec<W> load_term(const PartView& pv, int64_t t) {
-    TermRec<W> r;
-    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(pv.term + t * 4 * W);
+__device__ __forceinline__ void load_test(TermRec<W>& r, const PartView& pv, int64_t t) {
 #pragma unroll
-    for (int k = 0; k < 2 * W; ++k) {
-        ulonglong2 v = __ldg(p + k);
-        r.m[2 * k] = v.x;
-        r.m[2 * k + 1] = v.y;
+    for (int q = 0; q < W; ++q) {
+        const ulonglong2 v = __ldg(pv.test + (int64_t)q * pv.stride + t);
+        r.m[4 * q] = v.x;
+        r.m[4 * q + 1] = v.y;
     }
-    return r;
+}
+
+// The apply pair of every word of term t (into m[4q + 2], m[4q + 3]).
+template <int W>
+__device__ __forceinline__ void load_apply(TermRec<W>& r, const PartView& pv, int64_t t) {
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        const ulonglong2 v = __ldg(pv.apply + (int64_t)q * pv.stride + t);
+        r.m[4 * q + 2] = v.x;
+        r.m[4 * q + 3] = v.y;
+    }
 }
 
 // Hits of batched visitors wait in a per-warp shared queue until 32 have
@@ -459,8 +493,10 @@ __device__ __forceinline__ void queue_push(const V& v, typename V::Acc& acc, Hit
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
                                           int64_t t, int2& h) {
-    TermRec<W> r = load_term<W>(pv, t);
+    TermRec<W> r;
+    load_test<W>(r, pv, t);
     if (!r.applies(c)) return false;
+    load_apply<W>(r, pv, t);
     Key<W> img;
     const int par = r.image(c, img);
     if (DIAG) {
@@ -516,13 +552,19 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
             const int t0 = base + lane, t1 = base + 32 + lane;
             TermRec<W> r0, r1;
             const bool in0 = t0 < se.y, in1 = t1 < se.y;
-            if (in0) r0 = load_term<W>(pv, t0);
-            if (in1) r1 = load_term<W>(pv, t1);
+            if (in0) load_test<W>(r0, pv, t0);
+            if (in1) load_test<W>(r1, pv, t1);
+            // the apply pairs are loaded with the test pairs (not after the
+            // test), so that no load waits on the test's result
+            if (in0) load_apply<W>(r0, pv, t0);
+            if (in1) load_apply<W>(r1, pv, t1);
+            const bool app0 = in0 && r0.applies(c);
+            const bool app1 = in1 && r1.applies(c);
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 const TermRec<W>& rec = half ? r1 : r0;
                 const int t = half ? t1 : t0;
-                const bool app = (half ? in1 : in0) && rec.applies(c);
+                const bool app = half ? app1 : app0;
                 const unsigned m = __ballot_sync(0xffffffffu, app);
                 if (m == 0) continue;
                 if (app) {
@@ -747,9 +789,7 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
             for (int ts = grp.x; ts < grp.y; ts += kTerms) {
                 const int cnt = grp.y - ts < kTerms ? grp.y - ts : kTerms;
                 __syncthreads();
-                const ulonglong2* from = reinterpret_cast<const ulonglong2*>(pv.term + (int64_t)ts * 4 * W);
-                ulonglong2* to = reinterpret_cast<ulonglong2*>(s_terms);
-                for (int k = threadIdx.x; k < cnt * 2 * W; k += kThreads) to[k] = __ldg(from + k);
+                stage_terms<W>(s_terms, pv, ts, cnt, threadIdx.x, kThreads);
                 __syncthreads();
                 for (int i = warp; i < nrows; i += kWarpsPerBlock) {
                     const int64_t u = r0 + s_rows[i];
@@ -874,11 +914,12 @@ struct RowSet {
     int* count;             // device int: number of unique keys
     int32_t* head;
     int32_t* pos;
-    uint64_t* slots;        // hash set over the unique keys
+    uint32_t* tags;         // hash set over the unique keys (rows[] index keys[])
+    uint32_t* rows;
     uint64_t slot_mask;
     SortScratch sort;
     int64_t n;
-    HashView hash() const { return HashView{slots, keys, slot_mask, hash_shift(slot_mask + 1)}; }
+    HashView hash() const { return HashView{tags, rows, keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>
@@ -894,7 +935,8 @@ int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s
 // per-key data is stored at the first row's index.
 struct HashRows {
     uint64_t* keys;     // n x W, row order
-    uint64_t* slots;
+    uint32_t* tags;
+    uint32_t* rows;
     uint64_t slot_mask;
     int32_t* first;     // n
     int32_t* unique;    // n (first *count valid)
@@ -903,7 +945,7 @@ struct HashRows {
     int* count;
     int32_t* scan;      // scan scratch
     int64_t n;
-    HashView hash() const { return HashView{slots, keys, slot_mask, hash_shift(slot_mask + 1)}; }
+    HashView hash() const { return HashView{tags, rows, keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>

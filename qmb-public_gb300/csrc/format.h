@@ -34,12 +34,18 @@
 // Terms are stored sorted by group (stable in input order); groups[g] holds
 // [start, end); single_ne marks non-empty single groups and pair_ne[p] the
 // positions q > p whose pair group is non-empty.
+//
+// The per-word masks are stored word-major in two arrays, the test pair
+// (mask, val) and the apply pair (flip, par): lanes that read consecutive
+// terms of one word read consecutive 16-byte pairs (fully coalesced loads),
+// and a walk that tests terms one at a time reads the apply pair only for
+// terms whose test passed.
 #pragma once
 
 #include <stdint.h>
 
 #define QMBX_MAGIC 0x58424D51u  // "QMBX"
-#define QMBX_TABLE_VERSION 5u
+#define QMBX_TABLE_VERSION 6u
 #define QMBX_MAX_WORDS 4
 #define QMBX_ALIGN 256
 
@@ -47,7 +53,8 @@ enum { QMBX_PART_FWD = 0, QMBX_PART_ADJ = 1, QMBX_PART_DIAG = 2, QMBX_PARTS = 3 
 
 struct qmbx_table_part {
     int64_t n;            // terms in this part
-    uint64_t off_term;    // uint64[n][W][4] (mask, val, flip, par) per word
+    uint64_t off_test;    // uint64[W][n][2]: (mask, val) of word q of term t at (q * n + t) * 2
+    uint64_t off_apply;   // uint64[W][n][2]: (flip, par), same order
     uint64_t off_coef;    // double[n][2]   sign-folded coefficient
     uint64_t off_coef32;  // float[n][4]    (re_hi, re_lo, im_hi, im_lo)
     uint64_t off_orig;    // int32[n]       index of the term in the input table

@@ -143,8 +143,10 @@ void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     p.n = n;
     p.n_groups = qmbx_group_count(words);
     uint64_t un = (uint64_t)n;
-    p.off_term = cursor;
-    cursor = align_up(cursor + un * 4 * words * 8);
+    p.off_test = cursor;
+    cursor = align_up(cursor + un * 2 * words * 8);
+    p.off_apply = cursor;
+    cursor = align_up(cursor + un * 2 * words * 8);
     p.off_coef = cursor;
     cursor = align_up(cursor + un * 16);
     p.off_coef32 = cursor;
@@ -266,12 +268,14 @@ void count_terms(const int16_t* site, const uint8_t* kind, int64_t n_terms, int3
 
 void write_term(char* blob, const qmbx_table_part& p, int words, int64_t slot, const Compiled& c, const double* coef,
                 int64_t orig) {
-    uint64_t* rec = reinterpret_cast<uint64_t*>(blob + p.off_term) + slot * 4 * words;
+    uint64_t* test = reinterpret_cast<uint64_t*>(blob + p.off_test);
+    uint64_t* apply = reinterpret_cast<uint64_t*>(blob + p.off_apply);
     for (int w = 0; w < words; ++w) {
-        rec[4 * w + 0] = c.mask[w];
-        rec[4 * w + 1] = c.val[w];
-        rec[4 * w + 2] = c.flip[w];
-        rec[4 * w + 3] = c.par[w];
+        const uint64_t at = ((uint64_t)w * (uint64_t)p.n + (uint64_t)slot) * 2;
+        test[at] = c.mask[w];
+        test[at + 1] = c.val[w];
+        apply[at] = c.flip[w];
+        apply[at + 1] = c.par[w];
     }
     double re = coef[0], im = coef[1];
     if (c.pconst) {

@@ -43,7 +43,7 @@ def test_version_and_no_error(lib):
 
 
 class Part(ctypes.Structure):
-    _fields_ = [("n", ctypes.c_int64), ("off_term", ctypes.c_uint64), ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
+    _fields_ = [("n", ctypes.c_int64), ("off_test", ctypes.c_uint64), ("off_apply", ctypes.c_uint64), ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
                 ("off_norm", ctypes.c_uint64), ("off_groups", ctypes.c_uint64), ("off_single_ne", ctypes.c_uint64),
                 ("off_pair_ne", ctypes.c_uint64), ("off_nonempty", ctypes.c_uint64), ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
                 ("wide_groups", ctypes.c_int32), ("reserved", ctypes.c_int32)]
@@ -76,9 +76,9 @@ def read_part(blob, h, which):
     def arr(off, dtype, count):
         return np.frombuffer(blob, dtype=dtype, count=count, offset=off)
 
-    rec = arr(p.off_term, np.uint64, n * 4 * w).reshape(n, w, 4)
-    test = rec[:, :, 0:2]
-    apply = rec[:, :, 2:4]
+    # word-major: (mask, val) and (flip, par) of word q of term t at [q, t]
+    test = arr(p.off_test, np.uint64, n * 2 * w).reshape(w, n, 2).transpose(1, 0, 2)
+    apply = arr(p.off_apply, np.uint64, n * 2 * w).reshape(w, n, 2).transpose(1, 0, 2)
     coef = arr(p.off_coef, np.float64, n * 2).reshape(n, 2)
     orig = arr(p.off_orig, np.int32, n)
     return test, apply, coef, orig
