@@ -747,7 +747,10 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
     // the visitor's own shared memory comes out of the term staging area, so
     // the block stays within the 48 KB of static shared memory
     constexpr int kTerms = (kPivotTermBytes - 4 * V::kShared) / (32 * W);
-    __shared__ __align__(16) uint64_t s_terms[kTerms * 4 * W];
+    // word-major like the table: pair 2q + 0 (mask, val) and 2q + 1 (flip,
+    // par) of word q for term k at [2q + j][k], so that lanes reading
+    // consecutive terms read consecutive 16-byte pairs (no bank conflicts)
+    __shared__ ulonglong2 s_terms[2 * W][kTerms];
     __shared__ int32_t s_rows[kPivotRows];
     __shared__ int s_nrows;
     __shared__ int4 hitq[kWarpsPerBlock][64];
@@ -789,7 +792,15 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
             for (int ts = grp.x; ts < grp.y; ts += kTerms) {
                 const int cnt = grp.y - ts < kTerms ? grp.y - ts : kTerms;
                 __syncthreads();
-                stage_terms<W>(s_terms, pv, ts, cnt, threadIdx.x, kThreads);
+#pragma unroll
+                for (int q = 0; q < W; ++q) {
+                    const ulonglong2* test = pv.test + (int64_t)q * pv.stride + ts;
+                    const ulonglong2* apply = pv.apply + (int64_t)q * pv.stride + ts;
+                    for (int k = threadIdx.x; k < cnt; k += kThreads) {
+                        s_terms[2 * q][k] = __ldg(test + k);
+                        s_terms[2 * q + 1][k] = __ldg(apply + k);
+                    }
+                }
                 __syncthreads();
                 for (int i = warp; i < nrows; i += kWarpsPerBlock) {
                     const int64_t u = r0 + s_rows[i];
@@ -802,10 +813,9 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
                         bool hit = false;
                         if (k < cnt) {
                             TermRec<W> rec;
-                            const ulonglong2* sp = reinterpret_cast<const ulonglong2*>(s_terms + (int64_t)k * 4 * W);
 #pragma unroll
                             for (int q = 0; q < 2 * W; ++q) {
-                                const ulonglong2 x = sp[q];
+                                const ulonglong2 x = s_terms[q][k];
                                 rec.m[2 * q] = x.x;
                                 rec.m[2 * q + 1] = x.y;
                             }
