@@ -91,11 +91,13 @@ __device__ __forceinline__ bool key_eq(const Key<W>& a, const Key<W>& b) {
 // ---------------------------------------------------------------------------
 // open-addressing hash set over the keys of a row set
 //
-// Two parallel slot arrays: tags[i] is a 32-bit fingerprint of the key in
-// slot i (never all ones) and rows[i] the row holding it; both are all ones
-// when the slot is empty.  A lookup reads a bucket of four tags (16 bytes,
-// one L1 wavefront per lane) and touches rows[] and the key only on a tag
-// match, so an unsuccessful lookup costs one load.  Load factor <= 1/4.
+// Slots come in buckets of four; bucket j occupies 32 bytes (one L2 sector)
+// of the slot array: the four 32-bit fingerprints, then the four 32-bit rows.
+// A fingerprint is never all ones, and both words are all ones in an empty
+// slot.  A lookup reads the bucket's fingerprints with one 16-byte load (the
+// whole sector comes into L1 with it) and reads a row only on a fingerprint
+// match, so an unsuccessful lookup costs one load and a successful one finds
+// its row in L1.  Linear probing, load factor at most 1/4.
 // ---------------------------------------------------------------------------
 
 constexpr uint32_t kEmptyTag = 0xffffffffu;
@@ -111,26 +113,25 @@ __host__ __device__ __forceinline__ uint64_t key_hash(const Key<W>& k) {
 }
 
 struct HashView {
-    const uint32_t* tags;  // slot count
-    const uint32_t* rows;  // slot count
+    const uint32_t* slots; // 8 words per bucket (see above)
     const uint64_t* keys;  // keys of the set's rows, n x W
     uint64_t mask;         // slot count - 1 (a power of two minus one)
     int shift;             // 64 - log2(slot count / kBucket)
 };
 
-// Probing runs over 4-slot buckets: a key's home bucket is selected by the
-// top bits of its hash, and a lookup loads the bucket's four tags with one
-// 16-byte load; with the table at most a quarter full it almost always ends
-// in the home bucket.  Inserts fill the same sequence slot by slot, so a
-// bucket with an empty slot ends an unsuccessful search.
 constexpr int kBucket = 4;
 
-// Fingerprint stored in tags[]: the hash's high word, kept off the empty value.
+// Word offsets of slot i's fingerprint and row in the slot array.
+__host__ __device__ __forceinline__ uint64_t slot_tag_word(uint64_t i) { return (i >> 2) * 8 + (i & 3); }
+__host__ __device__ __forceinline__ uint64_t slot_row_word(uint64_t i) { return (i >> 2) * 8 + 4 + (i & 3); }
+
+// Fingerprint of a key: the hash's high word, kept off the empty value.
 __host__ __device__ __forceinline__ uint32_t hash_tag(uint64_t hv) {
     const uint32_t t = (uint32_t)(hv >> 32);
     return t == kEmptyTag ? kEmptyTag - 1u : t;
 }
 
+// First slot of a key's home bucket, selected by the top bits of its hash.
 __host__ __device__ __forceinline__ uint64_t hash_home(uint64_t hv, int shift) {
     return (hv >> shift) * (uint64_t)kBucket;
 }
@@ -141,21 +142,24 @@ __host__ __device__ __forceinline__ int hash_shift(uint64_t slots) {
     return s;
 }
 
-// Row stored for key (the first row holding it), or -1.
+// Row stored for key (the first row holding it), or -1.  Inserts fill the
+// probe sequence slot by slot, so a bucket with an empty slot ends an
+// unsuccessful search.
 template <int W>
 __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& key) {
     const uint64_t hv = key_hash<W>(key);
     const uint32_t fp = hash_tag(hv);
     uint64_t b = hash_home(hv, h.shift);
     for (uint64_t probe = 0; probe <= h.mask; probe += kBucket) {
-        const uint4 t4 = __ldg(reinterpret_cast<const uint4*>(h.tags + b));
+        const uint32_t* bucket = h.slots + 2 * b;
+        const uint4 t4 = __ldg(reinterpret_cast<const uint4*>(bucket));
         const uint32_t tag[kBucket] = {t4.x, t4.y, t4.z, t4.w};
         bool open = false;
 #pragma unroll
         for (int k = 0; k < kBucket; ++k) {
             open |= tag[k] == kEmptyTag;
             if (tag[k] == fp) {
-                const uint32_t row = __ldg(h.rows + b + k);
+                const uint32_t row = __ldg(bucket + kBucket + k);
                 if (row != kEmptyRow && key_eq<W>(load_key<W>(h.keys, (int64_t)row), key)) return (int64_t)row;
             }
         }
@@ -924,12 +928,11 @@ struct RowSet {
     int* count;             // device int: number of unique keys
     int32_t* head;
     int32_t* pos;
-    uint32_t* tags;         // hash set over the unique keys (rows[] index keys[])
-    uint32_t* rows;
+    uint64_t* slots;        // hash set over the unique keys
     uint64_t slot_mask;
     SortScratch sort;
     int64_t n;
-    HashView hash() const { return HashView{tags, rows, keys, slot_mask, hash_shift(slot_mask + 1)}; }
+    HashView hash() const { return HashView{reinterpret_cast<const uint32_t*>(slots), keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>
@@ -945,8 +948,7 @@ int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s
 // per-key data is stored at the first row's index.
 struct HashRows {
     uint64_t* keys;     // n x W, row order
-    uint32_t* tags;
-    uint32_t* rows;
+    uint64_t* slots;
     uint64_t slot_mask;
     int32_t* first;     // n
     int32_t* unique;    // n (first *count valid)
@@ -955,7 +957,7 @@ struct HashRows {
     int* count;
     int32_t* scan;      // scan scratch
     int64_t n;
-    HashView hash() const { return HashView{tags, rows, keys, slot_mask, hash_shift(slot_mask + 1)}; }
+    HashView hash() const { return HashView{reinterpret_cast<const uint32_t*>(slots), keys, slot_mask, hash_shift(slot_mask + 1)}; }
 };
 
 template <int W>

@@ -359,26 +359,21 @@ __global__ void compact_heads_kernel(const uint64_t* __restrict__ sorted, const 
 
 
 
-// Slot arrays of a hash set start all ones (empty).
-inline int clear_slots(uint32_t* tags, uint32_t* rows, uint64_t slot_mask, cudaStream_t s) {
-    QMBX_CUDA_TRY(cudaMemsetAsync(tags, 0xff, (slot_mask + 1) * sizeof(uint32_t), s));
-    QMBX_CUDA_TRY(cudaMemsetAsync(rows, 0xff, (slot_mask + 1) * sizeof(uint32_t), s));
-    return QMBX_OK;
-}
-
 template <int W>
 __global__ void hash_insert_kernel(const uint64_t* __restrict__ keys, const int* __restrict__ count,
-                                   uint32_t* __restrict__ tags, uint32_t* __restrict__ rows, uint64_t mask) {
+                                   uint64_t* __restrict__ slots, uint64_t mask) {
     int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= *count) return;
     Key<W> k = load_key<W>(keys, u);
     uint64_t hv = key_hash<W>(k);
     uint64_t i = hash_home(hv, hash_shift(mask + 1));
+    uint32_t* w = reinterpret_cast<uint32_t*>(slots);
     // the keys are unique and the table at most a quarter full, so an empty
-    // slot is reached within mask + 1 probes
+    // slot is reached within mask + 1 probes; a slot is claimed on its row
+    // word, then given its fingerprint
     for (uint64_t probe = 0; probe <= mask; ++probe) {
-        if (atomicCAS(rows + i, kEmptyRow, (uint32_t)u) == kEmptyRow) {
-            tags[i] = hash_tag(hv);
+        if (atomicCAS(w + slot_row_word(i), kEmptyRow, (uint32_t)u) == kEmptyRow) {
+            w[slot_tag_word(i)] = hash_tag(hv);
             return;
         }
         i = (i + 1) & mask;
@@ -401,8 +396,7 @@ RowSet take_rowset(Arena& ws, int64_t n) {
     out.pos = ws.take<int32_t>(cap);
     uint64_t slots = 64;
     while (slots < 4 * cap) slots <<= 1;
-    out.tags = ws.take<uint32_t>(slots);
-    out.rows = ws.take<uint32_t>(slots);
+    out.slots = ws.take<uint64_t>(slots);
     out.slot_mask = slots - 1;
     out.sort = take_sort_scratch<W>(ws, n);
     return out;
@@ -413,8 +407,9 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     const int64_t n = out.n;
     if (n == 0) {
         QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
+        QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
         QMBX_LAUNCH_CHECK("set_int_kernel");
-        return clear_slots(out.tags, out.rows, out.slot_mask, s);
+        return QMBX_OK;
     }
     int st;
     if ((st = pack_rows<W>(rows, n, nq, out.packed, s)) != QMBX_OK) return st;
@@ -423,8 +418,8 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.sort.scan, s)) != QMBX_OK) return st;
     QMBX_KERNEL(kGroupKeys, s, compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
                                                                        out.keys, out.first, out.start, out.count));
-    if ((st = clear_slots(out.tags, out.rows, out.slot_mask, s)) != QMBX_OK) return st;
-    QMBX_KERNEL(kGroupKeys, s, hash_insert_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.keys, out.count, out.tags, out.rows, out.slot_mask));
+    QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
+    QMBX_KERNEL(kGroupKeys, s, hash_insert_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.keys, out.count, out.slots, out.slot_mask));
     QMBX_LAUNCH_CHECK("build_rowset");
     return QMBX_OK;
 }
@@ -434,29 +429,32 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 
 // Insert every row; a key already present keeps the lowest row.  A slot is
-// claimed by a CAS on rows[] and then given its tag; a row that finds its
-// key in a claimed slot (compared in full: the tag may not be written yet)
-// lowers that slot's row with atomicMin.  Every row of a key therefore
-// meets the same slot, the first claimed on the key's probe sequence.
+// claimed by a CAS on its row word and then given its fingerprint; a row
+// that finds its key in a claimed slot (compared in full: the fingerprint
+// may not be written yet) lowers that slot's row with atomicMin.  Every row
+// of a key meets the same slot, the first claimed on the key's probe
+// sequence.
 template <int W>
-__global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ tags,
-                                       uint32_t* __restrict__ rows, uint64_t mask) {
+__global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint64_t* __restrict__ slots,
+                                       uint64_t mask) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const Key<W> k = load_key<W>(keys, r);
     const uint64_t hv = key_hash<W>(k);
     uint64_t i = hash_home(hv, hash_shift(mask + 1));
+    uint32_t* w = reinterpret_cast<uint32_t*>(slots);
     for (uint64_t probe = 0; probe <= mask; ++probe) {
-        uint32_t cur = *(volatile uint32_t*)(rows + i);
+        uint32_t* row = w + slot_row_word(i);
+        uint32_t cur = *(volatile uint32_t*)row;
         if (cur == kEmptyRow) {
-            cur = atomicCAS(rows + i, kEmptyRow, (uint32_t)r);
+            cur = atomicCAS(row, kEmptyRow, (uint32_t)r);
             if (cur == kEmptyRow) {
-                tags[i] = hash_tag(hv);
+                w[slot_tag_word(i)] = hash_tag(hv);
                 return;
             }
         }
         if (key_eq<W>(load_key<W>(keys, (int64_t)cur), k)) {
-            atomicMin(rows + i, (uint32_t)r);
+            atomicMin(row, (uint32_t)r);
             return;
         }
         i = (i + 1) & mask;
@@ -490,8 +488,7 @@ HashRows take_hashrows(Arena& ws, int64_t n) {
     out.keys = ws.take<uint64_t>(cap * W);
     uint64_t slots = 64;
     while (slots < 4 * cap) slots <<= 1;
-    out.tags = ws.take<uint32_t>(slots);
-    out.rows = ws.take<uint32_t>(slots);
+    out.slots = ws.take<uint64_t>(slots);
     out.slot_mask = slots - 1;
     out.first = ws.take<int32_t>(cap);
     out.unique = ws.take<int32_t>(cap);
@@ -505,16 +502,16 @@ HashRows take_hashrows(Arena& ws, int64_t n) {
 template <int W>
 int build_hashrows(const uint8_t* rows, int nq, HashRows& out, cudaStream_t s) {
     const int64_t n = out.n;
-    int st;
-    if ((st = clear_slots(out.tags, out.rows, out.slot_mask, s)) != QMBX_OK) return st;
+    QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
     if (n == 0) {
         QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
         QMBX_LAUNCH_CHECK("set_int_kernel");
         return QMBX_OK;
     }
+    int st;
     if ((st = pack_rows<W>(rows, n, nq, out.keys, s)) != QMBX_OK) return st;
     const unsigned grid = grid_for(n, kThreads);
-    QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.tags, out.rows, out.slot_mask));
+    QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.slots, out.slot_mask));
     QMBX_KERNEL(kGroupKeys, s, hashrows_resolve_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.hash(), out.first, out.head));
     if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.scan, s)) != QMBX_OK) return st;
     QMBX_KERNEL(kGroupKeys, s, hashrows_compact_kernel<<<grid, kThreads, 0, s>>>(out.head, out.pos, n, out.unique, out.count));
