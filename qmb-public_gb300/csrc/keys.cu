@@ -461,6 +461,16 @@ __global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_
     }
 }
 
+// Set the filter bits of every row's key.
+template <int W>
+__global__ void bloom_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ bloom,
+                                    uint32_t mask) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const uint64_t f = bloom_mix(key_hash<W>(load_key<W>(keys, r)));
+    atomicOr(bloom + bloom_word(f, mask), bloom_bits(f));
+}
+
 // first[r] = lowest row with row r's key; head[r] = (first[r] == r).
 template <int W>
 __global__ void hashrows_resolve_kernel(const uint64_t* __restrict__ keys, int64_t n, HashView h,
@@ -496,6 +506,8 @@ HashRows take_hashrows(Arena& ws, int64_t n) {
     out.pos = ws.take<int32_t>(cap);
     out.count = ws.take<int>(1);
     out.scan = ws.take<int32_t>((uint64_t)scan_scratch((int64_t)cap));
+    out.bloom_words = bloom_words_for(n);
+    out.bloom = out.bloom_words ? ws.take<uint32_t>(out.bloom_words) : nullptr;
     return out;
 }
 
@@ -511,6 +523,11 @@ int build_hashrows(const uint8_t* rows, int nq, HashRows& out, cudaStream_t s) {
     int st;
     if ((st = pack_rows<W>(rows, n, nq, out.keys, s)) != QMBX_OK) return st;
     const unsigned grid = grid_for(n, kThreads);
+    if (out.bloom_words) {
+        // complete before the first lookup (the resolve pass below)
+        QMBX_CUDA_TRY(cudaMemsetAsync(out.bloom, 0, (size_t)out.bloom_words * sizeof(uint32_t), s));
+        QMBX_KERNEL(kGroupKeys, s, bloom_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.bloom, out.bloom_words - 1));
+    }
     QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.slots, out.slot_mask));
     QMBX_KERNEL(kGroupKeys, s, hashrows_resolve_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.hash(), out.first, out.head));
     if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.scan, s)) != QMBX_OK) return st;
