@@ -490,7 +490,9 @@ def run_extra(args, wl) -> dict:
         line.update({"metric": "energy forward + backward step (FP32-compensated)", "value": ms32, "unit": "ms",
                      "higher_is_better": False, "fp64_ms": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
                      "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),
-                     "apply_term_applications_per_s": 2 * T * n / (prof["groups"]["enumerate"][1] / args.steps * 1e-3),
+                     "hermitian": ham._table(device, nq).hermitian,
+                     "walks_per_step": prof["groups"]["enumerate"][0] / args.steps,
+                     "apply_term_applications_per_s": prof["groups"]["enumerate"][0] * T * n / (prof["groups"]["enumerate"][1] * 1e-3),
                      "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]}})
     elif args.workload == "c4":
         psi32 = torch.from_numpy(wl["psi"]).to(torch.complex64).to(device)

@@ -72,6 +72,15 @@ int qmbx_table_build(const int16_t* site, const uint8_t* kind, const double* coe
 /* Counts read from a compiled table: [n_terms, live terms, diagonal terms, n_qubytes, particle_cut, n_words]. */
 int qmbx_table_counts(const void* table_host, int64_t counts[6]);
 
+/* *hermitian = 1 when the compiled operator equals its adjoint, else 0 (no
+ * counterpart in the reference).  The check compares the forward terms with
+ * the daggered, conjugated terms closed form by closed form (1e-12 relative
+ * to the largest coefficient) and requires the diagonal terms to sum to real
+ * coefficients; an operator written so that equal matrices have different
+ * closed forms can be reported 0 although Hermitian, never the reverse.
+ * Callers use it to get the gradient of <psi|H|psi> from H psi alone. */
+int qmbx_table_hermitian(const void* table_host, int32_t* hermitian);
+
 /* ---------------------------------------------------------------------------
  * apply_within: psi_j[j] = sum over terms t and rows i with t|i> = s|j> of
  * s * coef_t * psi_i[i].  Replaces apply_within_interface

@@ -35,6 +35,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_table_bytes": (ctypes.c_int, [_P, _P, _I64, _I32, _I32, _PU64]),
     "qmbx_table_build": (ctypes.c_int, [_P, _P, _P, _I64, _I32, _I32, _P, _U64]),
     "qmbx_table_counts": (ctypes.c_int, [_P, _PI64]),
+    "qmbx_table_hermitian": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     "qmbx_apply_within_workspace": (ctypes.c_int, [_P, _I64, _I64, _PU64]),
     "qmbx_apply_within": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P, _U64, _P]),
     "qmbx_apply_within_static": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P]),

@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/qmbx.h"
@@ -380,5 +382,87 @@ extern "C" int qmbx_table_counts(const void* table_host, int64_t counts[6]) {
     counts[3] = h->n_qubytes;
     counts[4] = h->particle_cut;
     counts[5] = h->n_words;
+    return QMBX_OK;
+}
+
+namespace qmbx {
+namespace {
+
+// 128-bit fingerprint of a canonical closed form (two independent 64-bit
+// mixes of its words): distinct forms collide with probability ~n^2 / 2^129.
+struct FormKey {
+    uint64_t a, b;
+    bool operator==(const FormKey& o) const { return a == o.a && b == o.b; }
+};
+struct FormKeyHash {
+    size_t operator()(const FormKey& k) const { return (size_t)(k.a ^ (k.b * 0x9E3779B97F4A7C15ull)); }
+};
+
+uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 27;
+    x *= 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Accumulate sign * coef of every term of a part under its canonical closed
+// form: the parity bits inside the mask are fixed by val on every row the
+// term applies to, so they move into the sign and leave the mask.
+void accumulate(const char* blob, const qmbx_table_part& p, int words, bool conj, double sign,
+                std::unordered_map<FormKey, std::pair<double, double>, FormKeyHash>& acc, double& scale) {
+    const uint64_t* test = reinterpret_cast<const uint64_t*>(blob + p.off_test);
+    const uint64_t* apply = reinterpret_cast<const uint64_t*>(blob + p.off_apply);
+    const double* coef = reinterpret_cast<const double*>(blob + p.off_coef);
+    for (int64_t t = 0; t < p.n; ++t) {
+        uint64_t ka = 0x243F6A8885A308D3ull, kb = 0x13198A2E03707344ull;
+        int parity = 0;
+        for (int q = 0; q < words; ++q) {
+            const uint64_t at = ((uint64_t)q * (uint64_t)p.n + (uint64_t)t) * 2;
+            const uint64_t mask = test[at], val = test[at + 1] & mask, flip = apply[at], par = apply[at + 1];
+            parity ^= __builtin_popcountll(val & par & mask) & 1;
+            const uint64_t form[4] = {mask, val, flip, par & ~mask};
+            for (int k = 0; k < 4; ++k) {
+                ka = mix64(ka ^ form[k]);
+                kb = mix64(kb + form[k] * 0xD6E8FEB86659FD93ull);
+            }
+        }
+        const double s = parity ? -sign : sign;
+        const double re = coef[2 * t], im = conj ? -coef[2 * t + 1] : coef[2 * t + 1];
+        std::pair<double, double>& v = acc[FormKey{ka, kb}];
+        v.first += s * re;
+        v.second += s * im;
+        scale = std::fmax(scale, std::fabs(re) + std::fabs(im));
+    }
+}
+
+}  // namespace
+}  // namespace qmbx
+
+extern "C" int qmbx_table_hermitian(const void* table_host, int32_t* hermitian) {
+    clear_error();
+    const qmbx_table_header* h = static_cast<const qmbx_table_header*>(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC || h->version != QMBX_TABLE_VERSION) {
+        return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    }
+    if (hermitian == nullptr) return fail(QMBX_ERR_ARGUMENT, "hermitian must not be NULL");
+    const char* blob = static_cast<const char*>(table_host);
+    // H = sum of forward terms; H^dagger = sum of the daggered terms with
+    // conjugated coefficients.  H is Hermitian when both sums agree form by
+    // form, and the diagonal terms sum to a real coefficient per form.
+    std::unordered_map<FormKey, std::pair<double, double>, FormKeyHash> off, diag;
+    double scale = 0.0;
+    accumulate(blob, h->part[QMBX_PART_FWD], h->n_words, false, 1.0, off, scale);
+    accumulate(blob, h->part[QMBX_PART_ADJ], h->n_words, true, -1.0, off, scale);
+    accumulate(blob, h->part[QMBX_PART_DIAG], h->n_words, false, 1.0, diag, scale);
+    const double tol = 1e-12 * (scale > 0.0 ? scale : 1.0);
+    int32_t ok = 1;
+    for (const auto& kv : off) {
+        if (std::fabs(kv.second.first) > tol || std::fabs(kv.second.second) > tol) ok = 0;
+    }
+    for (const auto& kv : diag) {
+        if (std::fabs(kv.second.second) > tol) ok = 0;
+    }
+    *hermitian = ok;
     return QMBX_OK;
 }

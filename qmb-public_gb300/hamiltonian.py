@@ -70,6 +70,16 @@ class _Table:
         counts = (ctypes.c_int64 * 6)()
         _native.check(lib.qmbx_table_counts(self.host.data_ptr(), counts))
         self.n_terms, self.n_live, self.n_diag, self.n_qubytes, self.particle_cut, self.n_words = list(counts)
+        self._hermitian: bool | None = None
+
+    @property
+    def hermitian(self) -> bool:
+        """Whether the compiled operator equals its adjoint (checked once, on the host)."""
+        if self._hermitian is None:
+            flag = ctypes.c_int32()
+            _native.check(_native.library().qmbx_table_hermitian(self.host.data_ptr(), ctypes.byref(flag)))
+            self._hermitian = bool(flag.value)
+        return self._hermitian
 
     @property
     def h(self) -> int:

@@ -229,3 +229,43 @@ def test_dead_terms_are_dropped(lib):
     counts = (ctypes.c_int64 * 6)()
     native.check(lib.qmbx_table_counts(blob.ctypes.data, counts))
     assert list(counts) == [3, 2, 1, 1, 1, 1]
+
+
+def hermitian_flag(lib, site, kind, coef, nq, pc):
+    blob = compile_table(lib, site, kind, coef, nq, pc)
+    flag = ctypes.c_int32()
+    native.check(lib.qmbx_table_hermitian(blob.ctypes.data, ctypes.byref(flag)))
+    return flag.value
+
+
+@pytest.mark.parametrize("case", ["ab_initio_6", "ab_initio_10_complex", "random_terms_fermi", "random_terms_bose2",
+                                  "ising_4x4", "hubbard_3x2"])
+def test_hermitian_flag_agrees_with_the_dense_matrix(lib, case):
+    g = golden(case)
+    pc = int(g["particle_cut"])
+    rows = np.concatenate([g["configs_i"], g["configs_j"]])[:150]
+    rows = np.unique(rows, axis=0)
+    flag = hermitian_flag(lib, g["site"], g["kind"], g["coef"], rows.shape[1], pc)
+    h = oracle.dense_matrix(g["site"], g["kind"], g["coef"], rows, pc)
+    gap = np.abs(h - h.conj().T).max()
+    if flag:
+        # a principal block of a Hermitian operator is Hermitian
+        assert gap <= 1e-12 * max(1.0, np.abs(h).max())
+    else:
+        assert gap > 1e-6
+
+
+def test_hermitian_flag_on_written_out_operators(lib):
+    site = np.array([[0, 1, 0, 0], [1, 0, 0, 0], [2, 2, 0, 0]], dtype=np.int16)
+    kind = np.array([[1, 0, 2, 2], [1, 0, 2, 2], [1, 0, 2, 2]], dtype=np.uint8)
+    # a+_0 a_1 + a+_1 a_0 + 0.5 n_2 is Hermitian; with i and -i on the hops too
+    assert hermitian_flag(lib, site, kind, np.array([[1.0, 0], [1.0, 0], [0.5, 0]]), 1, 1) == 1
+    assert hermitian_flag(lib, site, kind, np.array([[0, 1.0], [0, -1.0], [0.5, 0]]), 1, 1) == 1
+    # i on both hops, or a complex diagonal coefficient, is not
+    assert hermitian_flag(lib, site, kind, np.array([[0, 1.0], [0, 1.0], [0.5, 0]]), 1, 1) == 0
+    assert hermitian_flag(lib, site, kind, np.array([[1.0, 0], [1.0, 0], [0.5, 0.5]]), 1, 1) == 0
+    # the second hop written in the other order: -a_0 a+_1 is the same operator as a+_1 a_0
+    site2 = np.array([[0, 1, 0, 0], [0, 1, 0, 0], [2, 2, 0, 0]], dtype=np.int16)
+    kind2 = np.array([[1, 0, 2, 2], [0, 1, 2, 2], [1, 0, 2, 2]], dtype=np.uint8)
+    assert hermitian_flag(lib, site2, kind2, np.array([[1.0, 0], [-1.0, 0], [0.5, 0]]), 1, 1) == 1
+    assert hermitian_flag(lib, site2, kind2, np.array([[1.0, 0], [1.0, 0], [0.5, 0]]), 1, 1) == 0
