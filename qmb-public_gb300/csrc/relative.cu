@@ -7,12 +7,18 @@
 //
 //   find_relative  pass 1 counts the candidate records per weight bucket (the
 //                  top 12 bits of an FP32 estimate |coef|^2 |psi|^2 of the
-//                  weight); the host picks the bucket that holds the
-//                  count_selected-th record; pass 2 re-enumerates and keeps
-//                  only records at or above the bucket below it, now with the
-//                  exact FP64 weight of the reference (:494-497); a radix
-//                  sort ranks them by (weight, visiting order) and the first
-//                  count_selected are sorted and de-duplicated by row.
+//                  weight) over every 16th source row; the host picks from
+//                  the scaled counts a bucket that should hold about twice
+//                  count_selected records above it; pass 2 enumerates every
+//                  row, counts all records per bucket and keeps those at or
+//                  above the bucket below the chosen one, now with the exact
+//                  FP64 weight of the reference (:494-497).  The exact counts
+//                  of pass 2 then confirm that every record down to the
+//                  count_selected-th was kept (else pass 2 runs again with
+//                  the exact threshold); a radix sort ranks the kept records
+//                  by (weight, visiting order) and the first count_selected
+//                  are sorted and de-duplicated by row.  Small inputs count
+//                  every row in pass 1 and need no confirmation.
 //   single_relative  one thread per row keeps the best Efraimidis-Spirakis
 //                  key of its candidates in registers.
 #include <cuda_runtime.h>
@@ -67,24 +73,21 @@ struct RelativeArgs {
 template <int W, bool EMIT>
 struct RelativeVisitor : VisitorBase {
     RelativeArgs a;
-    static constexpr int kShared = EMIT ? 0 : kBuckets;
+    static constexpr int kShared = kBuckets;
     struct Acc {
         double2 p;
         float m;
         int64_t row;
         int* hist;
     };
+    // both passes count every record per bucket (pass 2's counts confirm pass 1's choice)
     __device__ __forceinline__ void block_init(int* sh) const {
-        if (!EMIT) {
-            for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) sh[k] = 0;
-        }
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) sh[k] = 0;
     }
     __device__ __forceinline__ void block_flush(int* sh) const {
-        if (!EMIT) {
-            for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
-                int v = sh[k];
-                if (v) atomicAdd(a.hist + k, (unsigned long long)v);
-            }
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) {
+            int v = sh[k];
+            if (v) atomicAdd(a.hist + k, (unsigned long long)v);
         }
     }
     __device__ __forceinline__ void init(Acc& acc, int64_t row, const Key<W>&, int* sh) const {
@@ -99,10 +102,8 @@ struct RelativeVisitor : VisitorBase {
     __device__ __forceinline__ void record(Acc& acc, const Key<W>& img, const PartView& pv, int parity,
                                            int64_t slot) const {
         const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
-        if (!EMIT) {
-            atomicAdd(&acc.hist[b], 1);
-            return;
-        }
+        atomicAdd(&acc.hist[b], 1);
+        if (!EMIT) return;
         if (b < a.emit_from) return;
         const double w = exact_weight(__ldg(pv.coef + slot), acc.p, parity);
         if (w == 0.0) return;
@@ -166,6 +167,35 @@ __global__ void gather_selected_kernel(const int32_t* __restrict__ order, const 
     for (int q = 0; q < W; ++q) out[i * W + q] = keys[src * W + q];
 }
 
+// Inputs of 4,096 rows or more count records on every kSampleStride-th row
+// in pass 1.
+constexpr int64_t kSampleStride = 16;
+constexpr int64_t kSampleMinRows = 4096;
+
+// Every kSampleStride-th row of keys and psi.
+template <int W>
+__global__ void sample_rows_kernel(const uint64_t* __restrict__ keys, const double2* __restrict__ psi, int64_t n_s,
+                                   uint64_t* __restrict__ keys_s, double2* __restrict__ psi_s) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_s) return;
+    const int64_t r = j * kSampleStride;
+#pragma unroll
+    for (int q = 0; q < W; ++q) keys_s[j * W + q] = keys[r * W + q];
+    psi_s[j] = psi[r];
+}
+
+// Highest bucket b whose buckets >= b hold at least `target` records
+// (counts scaled by `scale`): the bucket of the target-th heaviest record;
+// 0 when all buckets above 0 hold fewer.
+int bucket_above(const std::vector<unsigned long long>& hist, double scale, double target) {
+    double above = 0.0;
+    for (int b = kBuckets - 1; b >= 1; --b) {
+        above += scale * (double)hist[b];
+        if (above >= target) return b;
+    }
+    return 0;
+}
+
 __global__ void zero_u64_kernel(unsigned long long* p, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = 0;
@@ -190,6 +220,8 @@ template <int W>
 struct FindLayout {
     HashRows excl;
     uint64_t* keys_i;
+    uint64_t* keys_s;       // every kSampleStride-th row of keys_i
+    double2* psi_s;         // and its amplitude
     unsigned long long* hist;
     unsigned long long* n_emit;
     int* overflow;
@@ -204,16 +236,13 @@ struct FindLayout {
 };
 
 template <int W>
-uint64_t record_bytes() {
-    // rank key (16 B) + image key (8W) + sorted copy (16 B) + order (4 B) + sort scratch (16 + 4 B), rounded up
-    return 16 + 8 * W + 16 + 4 + 16 + 4 + 8;
-}
-
-template <int W>
 FindLayout<W> take_find(Arena& ws, int64_t n_i, int64_t k, int64_t n_ex, int64_t cap) {
     FindLayout<W> L;
     L.excl = take_hashrows<W>(ws, n_ex);
     L.keys_i = ws.take<uint64_t>((uint64_t)(n_i > 0 ? n_i : 1) * W);
+    const int64_t n_s = n_i / kSampleStride + 1;
+    L.keys_s = ws.take<uint64_t>((uint64_t)n_s * W);
+    L.psi_s = ws.take<double2>((uint64_t)n_s);
     L.hist = ws.take<unsigned long long>(kBuckets + 1);
     L.n_emit = L.hist + kBuckets;
     L.overflow = ws.take<int>(1);
@@ -234,18 +263,25 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     const qmbx_table_header* h = header_of(a.table_host);
     const int nq = h->n_qubytes;
     const int64_t k = a.k;
-    // initial emission capacity: what the workspace can hold
-    Arena probe(nullptr, 0);
-    take_find<W>(probe, a.n_i, k, a.n_ex, 1);
-    uint64_t fixed = probe.used;
-    int64_t cap = 1;
-    if (workspace_bytes > fixed) cap = (int64_t)((workspace_bytes - fixed) / (2 * record_bytes<W>())) + 1;
-    for (;;) {
+    // emission capacity: the most records the workspace can hold (the
+    // layout grows monotonically with the capacity, so bisect), such that a
+    // workspace sized for c records by this layout holds at least c
+    auto fits = [&](int64_t c) {
         Arena trial(nullptr, 0);
-        take_find<W>(trial, a.n_i, k, a.n_ex, cap);
-        if (trial.used <= workspace_bytes || cap == 1) break;
-        cap = cap * 3 / 4;
-        if (cap < 1) cap = 1;
+        take_find<W>(trial, a.n_i, k, a.n_ex, c);
+        return trial.used <= workspace_bytes;
+    };
+    int64_t cap = 1;
+    if (fits(1)) {
+        int64_t hi = (int64_t)(workspace_bytes / 16) + 2;  // a record takes more than 16 bytes
+        while (cap < hi) {
+            const int64_t mid = cap + (hi - cap + 1) / 2;
+            if (fits(mid)) {
+                cap = mid;
+            } else {
+                hi = mid - 1;
+            }
+        }
     }
     Arena ws(workspace, workspace_bytes);
     FindLayout<W> L = take_find<W>(ws, a.n_i, k, a.n_ex, cap);
@@ -269,47 +305,96 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
-    if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
-
     std::vector<unsigned long long> hist(kBuckets);
-    QMBX_CUDA_TRY(cudaMemcpyAsync(hist.data(), L.hist, kBuckets * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-    // bucket holding the k-th heaviest record (records with a zero estimate
-    // sit in bucket 0 and are emitted only when fewer than k records lie above)
-    unsigned long long above = 0;
-    int b_k = 0;
-    for (int b = kBuckets - 1; b >= 1; --b) {
-        above += hist[b];
-        if (above >= (unsigned long long)k) {
-            b_k = b;
-            break;
-        }
-    }
-    int emit_from = b_k > 1 ? b_k - 1 : 0;
-    unsigned long long need = 0;
-    for (int b = emit_from; b < kBuckets; ++b) need += hist[b];
-    if ((int64_t)need > cap) {
+    auto read_hist = [&]() -> int {
+        QMBX_CUDA_TRY(cudaMemcpyAsync(hist.data(), L.hist, kBuckets * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+        return QMBX_OK;
+    };
+    auto need_bytes = [&](unsigned long long records) {
         Arena want(nullptr, 0);
-        take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)need);
-        if (needed) *needed = want.used;
-        return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
-                    (unsigned long long)want.used, need);
+        take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)records);
+        return want.used;
+    };
+    // records with a zero estimate sit in bucket 0 and are emitted only when
+    // fewer than k records lie above
+    auto records_from = [&](int from) {
+        unsigned long long n = 0;
+        for (int b = from; b < kBuckets; ++b) n += hist[b];
+        return n;
+    };
+
+    // pass 1: bucket counts over every row, or every kSampleStride-th row of large inputs
+    const bool sampled = a.n_i >= kSampleMinRows;
+    int emit_from;
+    if (sampled) {
+        const int64_t n_s = (a.n_i + kSampleStride - 1) / kSampleStride;
+        QMBX_KERNEL(kGroupOther, s, sample_rows_kernel<W><<<grid_for(n_s, kThreads), kThreads, 0, s>>>(L.keys_i, r.psi, n_s, L.keys_s, L.psi_s));
+        QMBX_LAUNCH_CHECK("sample_rows_kernel");
+        RelativeArgs rs = r;
+        rs.psi = L.psi_s;
+        rs.n_i = n_s;
+        if ((st = launch_relative<W, false>(rs, L.keys_s, n_s, s)) != QMBX_OK) return st;
+        if ((st = read_hist()) != QMBX_OK) return st;
+        // aim at about twice k records above the chosen bucket, one more bucket of slack
+        const int b_est = bucket_above(hist, (double)a.n_i / (double)n_s, 2.0 * (double)k);
+        emit_from = b_est > 1 ? b_est - 1 : 0;
+        const double est = (double)a.n_i / (double)n_s * (double)records_from(emit_from);
+        if (est > (double)cap) {
+            if (needed) *needed = need_bytes((unsigned long long)(1.5 * est) + 1);
+            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for about %.0f records near the threshold",
+                        (unsigned long long)need_bytes((unsigned long long)(1.5 * est) + 1), est);
+        }
+        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
+    } else {
+        if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
+        if ((st = read_hist()) != QMBX_OK) return st;
+        const int b_k = bucket_above(hist, 1.0, (double)k);
+        emit_from = b_k > 1 ? b_k - 1 : 0;
+        const unsigned long long need = records_from(emit_from);
+        if ((int64_t)need > cap) {
+            if (needed) *needed = need_bytes(need);
+            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
+                        (unsigned long long)need_bytes(need), need);
+        }
+        if (need == 0) return QMBX_OK;
+        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
     }
-    if (need == 0) return QMBX_OK;
-    r.emit_from = emit_from;
+
+    // pass 2: emit the records at or above emit_from; count every record per bucket
     r.n_emit = L.n_emit;
     r.cap_emit = cap;
     r.emit_rank = L.emit_rank;
     r.emit_keys = L.emit_keys;
     r.overflow = L.overflow;
-    if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
     unsigned long long n_emit = 0;
-    int overflow = 0;
-    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
-    QMBX_CUDA_TRY(cudaMemcpyAsync(&overflow, L.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
-    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-    if (overflow || (int64_t)n_emit > cap) {
-        return fail(QMBX_ERR_DEVICE, "find_relative emitted %llu records into room for %lld", n_emit, (long long)cap);
+    for (int attempt = 0;; ++attempt) {
+        r.emit_from = emit_from;
+        if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
+        int overflow = 0;
+        QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
+        QMBX_CUDA_TRY(cudaMemcpyAsync(&overflow, L.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+        if ((st = read_hist()) != QMBX_OK) return st;
+        // the exact threshold from pass 2's full counts
+        const int b_k = bucket_above(hist, 1.0, (double)k);
+        const int exact_from = b_k > 1 ? b_k - 1 : 0;
+        const unsigned long long need = records_from(exact_from < emit_from ? exact_from : emit_from);
+        if (overflow || (int64_t)n_emit > cap) {
+            if (needed) *needed = need_bytes(need);
+            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
+                        (unsigned long long)need_bytes(need), need);
+        }
+        if (emit_from <= exact_from) break;  // every record down to the k-th was kept
+        if (attempt > 0) return fail(QMBX_ERR_DEVICE, "find_relative threshold did not settle");
+        // the sampled counts put the threshold too high: again with the exact one
+        emit_from = exact_from;
+        if ((int64_t)records_from(emit_from) > cap) {
+            if (needed) *needed = need_bytes(records_from(emit_from));
+            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
+                        (unsigned long long)need_bytes(records_from(emit_from)), records_from(emit_from));
+        }
+        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
+        QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
     }
     if (n_emit == 0) return QMBX_OK;
     const int64_t e = (int64_t)n_emit;

@@ -136,3 +136,16 @@ def test_find_relative_exact_on_seed_subset_of_c5(workloads, cuda_device):
                             torch.from_numpy(wl["configs_i"]).to(cuda_device)).cpu().numpy()
     assert want.shape[0] > 1000
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("k", [7, 300, 20000, 1 << 22])
+def test_find_relative_with_sampled_threshold(k, cuda_device):
+    # 6,000 source rows: pass 1 counts every 16th row and pass 2 confirms
+    site, kind, coef = (x.numpy() for x in __import__("qmb_gb300").terms.integral_hamiltonian_tables(9, seed=3))
+    rows = __import__("qmb_gb300").terms.random_determinants(9, 4, 4, 6000, seed=8)
+    rng = np.random.default_rng(k)
+    psi = rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])
+    ham = Hamiltonian((torch.from_numpy(site), torch.from_numpy(kind), torch.from_numpy(coef)), kind="fermi")
+    want, _ = oracle.find_relative(site, kind, coef, rows, psi, k, rows, 1, rule="ranked")
+    got = ham.find_relative(torch.from_numpy(rows).to(cuda_device), torch.from_numpy(psi).to(cuda_device), k).cpu().numpy()
+    assert np.array_equal(got, want)
