@@ -644,34 +644,39 @@ __device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& a
 // pair groups (p, q) with q occupied.  Warp-uniform state; next() yields one
 // group id at a time so the walk has a single call site (small code, few
 // registers).
+// Word i of a W-word array, selected without indexing the array by a
+// runtime value (which would put it in local memory).
+template <int W>
+__device__ __forceinline__ uint64_t pick_word(const uint64_t (&a)[W], int i) {
+    uint64_t r = a[0];
+#pragma unroll
+    for (int q = 1; q < W; ++q) r = (q == i) ? a[q] : r;
+    return r;
+}
+
 template <int W>
 struct GroupCursor {
-    const Key<W>* c;
-    const uint64_t* single_ne;
-    const uint64_t* pair_ne;
     int first;        // -2: group 0 pending; -1: single level; >= 0: pair level with this first position
     int word;         // word of the partner mask being drained
     uint64_t bits;    // partner bits still to yield in `word`
     uint64_t occ[W];  // occupied positions not yet used as `first`
 
-    __device__ __forceinline__ void start(const Key<W>& row, const PartView& pv) {
-        c = &row;
-        single_ne = pv.single_ne;
-        pair_ne = pv.pair_ne;
+    __device__ __forceinline__ void start(const Key<W>& row) {
         first = -2;
         word = 0;
         bits = 0;
 #pragma unroll
         for (int q = 0; q < W; ++q) occ[q] = row.w[q];
     }
-    __device__ __forceinline__ uint64_t partners(int r) const {
-        return c->w[r] & (first < 0 ? __ldg(single_ne + r) : __ldg(pair_ne + (int64_t)first * W + r));
+    __device__ __forceinline__ uint64_t partners(const Key<W>& row, const PartView& pv, int r) const {
+        return pick_word<W>(row.w, r) &
+               (first < 0 ? __ldg(pv.single_ne + r) : __ldg(pv.pair_ne + (int64_t)first * W + r));
     }
-    __device__ __forceinline__ bool next(int64_t& g) {
+    __device__ __forceinline__ bool next(int64_t& g, const Key<W>& row, const PartView& pv) {
         if (first == -2) {
             first = -1;
             word = 0;
-            bits = partners(0);
+            bits = partners(row, pv, 0);
             g = 0;
             return true;
         }
@@ -686,19 +691,20 @@ struct GroupCursor {
             }
             if (word + 1 < W) {
                 ++word;
-                bits = partners(word);
+                bits = partners(row, pv, word);
                 continue;
             }
-            // next first position (pair level)
-            int q = 0;
-#pragma unroll 1
-            while (q < W && occ[q] == 0) ++q;
+            // next first position (pair level): the lowest occupied position left
+            int q = W;
+#pragma unroll
+            for (int k = W - 1; k >= 0; --k) q = occ[k] ? k : q;
             if (q == W) return false;
-            const int b = __ffsll((long long)occ[q]) - 1;
-            occ[q] &= occ[q] - 1;
-            first = 64 * q + b;
+            const uint64_t w = pick_word<W>(occ, q);
+#pragma unroll
+            for (int k = 0; k < W; ++k) occ[k] = (k == q) ? occ[k] & (occ[k] - 1) : occ[k];
+            first = 64 * q + (__ffsll((long long)w) - 1);
             word = q;  // partners sit at higher positions
-            bits = partners(word);
+            bits = partners(row, pv, word);
         }
     }
 };
@@ -708,16 +714,16 @@ __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, cons
                                           int lane, HitQueue& hq) {
     if (pv.n == 0) return;
     GroupCursor<W> cur;
-    cur.start(c, pv);
+    cur.start(c);
     int64_t g;
     if (pv.wide) {
 #pragma unroll 1
-        while (cur.next(g)) walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
+        while (cur.next(g, c, pv)) walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
     } else {
         // small groups: lane k takes every 32nd group of the sequence
         int k = 0;
 #pragma unroll 1
-        while (cur.next(g)) {
+        while (cur.next(g, c, pv)) {
             if (k == lane) walk_group_serial<W, DIAG>(v, acc, c, pv, g);
             k = (k + 1) & 31;
         }

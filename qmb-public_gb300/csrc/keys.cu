@@ -571,12 +571,10 @@ static int sm_count() {
 int pivot_grid() { return sm_count() * 4; }
 
 bool use_pivot_walk(const PartView& part) {
-    static int mode = -2;  // -1 automatic, 0 grouped, 1 pivot
-    if (mode == -2) {
-        const char* e = getenv("QMBX_WALK");
-        mode = (e != nullptr && e[0] == 'p') ? 1 : (e != nullptr && e[0] == 'g') ? 0 : -1;
-    }
-    if (mode >= 0) return mode == 1;
+    // QMBX_WALK=pivot or grouped overrides the choice (read at every call)
+    const char* e = getenv("QMBX_WALK");
+    if (e != nullptr && e[0] == 'p') return true;
+    if (e != nullptr && e[0] == 'g') return false;
     // groups holding hundreds of terms amortise staging them in shared memory
     return part.n_nonempty > 0 && part.n >= (int64_t)kPivotMeanGroup * part.n_nonempty;
 }

@@ -12,7 +12,7 @@ sizes are checked through properties that need only a small oracle run:
 * the adjoint identity <g, H psi> = <H^dagger g, psi> on random full vectors;
 * find_relative at C5 size: output sorted, unique, outside the excluded set,
   each row connected to the seeds; and bit-exact against the oracle's ranked
-  rule on a subset of seeds (full 3.1M-term table, the pivot walk).
+  rule on a subset of seeds (full 3.1M-term table, pivot and grouped walks).
 
 Workloads: C2 (28 spin orbitals, 55,371 terms, 20,000 x 200,000 rows), C4
 (Hubbard 8x8, 1,000,000 rows), C5 (76 spin orbitals, 3,076,435 terms, 8,192
@@ -123,7 +123,12 @@ def test_find_relative_invariants_at_c5_size(workloads, cuda_device):
     assert np.all(np.abs(hpsi) > 0)
 
 
-def test_find_relative_exact_on_seed_subset_of_c5(workloads, cuda_device):
+@pytest.mark.parametrize("walk", ["auto", "grouped"])
+def test_find_relative_exact_on_seed_subset_of_c5(workloads, walk, cuda_device, monkeypatch):
+    # the automatic choice takes the pivot walk here; "grouped" forces the
+    # warp-per-row walk over two key words
+    if walk != "auto":
+        monkeypatch.setenv("QMBX_WALK", walk)
     wl = workloads("c5")
     ham = wl["ham"]
     rng = np.random.default_rng(4)
