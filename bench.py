@@ -229,15 +229,41 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_traffic(workload: str):
-    """DRAM bytes per enumeration launch from the committed ncu summary, or None."""
+def ncu_figure(workload: str, name: str):
+    """A per-launch figure of the term walk (`name: value`) from the committed ncu summary, or None."""
     path = os.path.join(REPO, "profiles", f"term_walk_{workload}.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    m = re.search(name + r":\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per enumeration launch from the committed ncu summary, or None."""
+    return ncu_figure(workload, "traffic_bytes_per_launch")
+
+
+def issue_roofline(workload: str, launch_ms: float, device, clocks: dict):
+    """The walk's binding resource: warp instructions issued per second against the SMs' issue slots.
+
+    The walk is sparse integer work (bit tests, hashing, L2 lookups), so its
+    HBM fraction is small by construction; this second roofline divides the
+    warp instructions of one launch (ncu, committed summary) by the live
+    launch time, against 4 issue slots per SM per clock at the sampled clock.
+    """
+    import torch
+
+    inst = ncu_figure(workload, "warp_instructions_per_launch")
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if inst is None or not mhz or launch_ms <= 0:
+        return None
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    achieved = inst / (launch_ms * 1e-3)
+    peak = sms * 4 * mhz * 1e6
+    return {"achieved": achieved, "peak": peak, "unit": "warp-inst/s", "frac": achieved / peak,
+            "warp_instructions_per_launch": inst, "sms": sms, "sm_mhz": mhz}
 
 
 def run_ours(args, wl, rank: int, world: int) -> dict | None:
@@ -387,6 +413,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
                      "traffic": ncu_traffic(args.workload), "kernel": "term walk (grouped_kernel)",
                      "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_ms,
                      "peak_source": f"{peak_kind} hbm_gbs"},
+        "issue_roofline": issue_roofline(args.workload, per_launch_ms, device, clocks.summary()),
         "cpu_baseline": cpu,
         "e2e": {"value": world * units / (ms_e2e / args.steps * 1e-3), "unit": "term-applications/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
