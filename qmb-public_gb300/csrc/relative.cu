@@ -65,7 +65,8 @@ struct RelativeArgs {
     int emit_from;           // lowest bucket emitted
     unsigned long long* n_emit;
     int64_t cap_emit;
-    uint64_t* emit_rank;     // [cap][2]: ~weight bits, ~order
+    uint64_t* emit_rank;     // [cap][2]: (slot | part << 62 | parity << 63, row) from the walk;
+                             // (~weight bits, ~order) after rank_records_kernel
     uint64_t* emit_keys;     // [cap][W]
     int* overflow;
 };
@@ -92,42 +93,44 @@ struct RelativeVisitor : VisitorBase {
     }
     __device__ __forceinline__ void init(Acc& acc, int64_t row, const Key<W>&, int* sh) const {
         acc.p = __ldg(a.psi + row);
-        acc.m = (float)(acc.p.x * acc.p.x + acc.p.y * acc.p.y);
+        // FP32 estimate of |psi|^2 (no FP64 in the walk)
+        const float px = (float)acc.p.x, py = (float)acc.p.y;
+        acc.m = __fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py));
         acc.row = row;
         acc.hist = sh;
     }
     static constexpr bool kProbe = true;
     HashView lookup;  // the exclusion set
-    // A candidate record whose image is not excluded.
-    __device__ __forceinline__ void record(Acc& acc, const Key<W>& img, const PartView& pv, int parity,
+    // A candidate record whose image is not excluded.  The emission pass
+    // stores what identifies the record (term slot and part, parity, row);
+    // its exact FP64 weight is formed afterwards by rank_records_kernel, so
+    // that the walk issues no FP64 instruction.
+    __device__ __forceinline__ void record(Acc& acc, const Key<W>& img, const PartView& pv, int part, int parity,
                                            int64_t slot) const {
         const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
         atomicAdd(&acc.hist[b], 1);
         if (!EMIT) return;
         if (b < a.emit_from) return;
-        const double w = exact_weight(__ldg(pv.coef + slot), acc.p, parity);
-        if (w == 0.0) return;
         const unsigned long long at = atomicAdd(a.n_emit, 1ull);
         if ((int64_t)at >= a.cap_emit) {
             *a.overflow = 1;
             return;
         }
-        const uint64_t order = (uint64_t)__ldg(pv.orig + slot) * (uint64_t)a.n_i + (uint64_t)acc.row;
-        a.emit_rank[2 * at + 0] = ~(uint64_t)__double_as_longlong(w);
-        a.emit_rank[2 * at + 1] = ~order;
+        a.emit_rank[2 * at + 0] = (uint64_t)slot | ((uint64_t)part << 62) | ((uint64_t)parity << 63);
+        a.emit_rank[2 * at + 1] = (uint64_t)acc.row;
 #pragma unroll
         for (int q = 0; q < W; ++q) a.emit_keys[at * W + q] = img.w[q];
     }
     __device__ __forceinline__ bool take(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
                                          int64_t pos, int2&) const {
-        if (pos < 0) record(acc, img, a.off, parity, slot);
+        if (pos < 0) record(acc, img, a.off, 0, parity, slot);
         return false;
     }
     __device__ __forceinline__ void visit(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        if (hash_find<W>(lookup, img) < 0) record(acc, img, a.off, parity, slot);
+        if (hash_find<W>(lookup, img) < 0) record(acc, img, a.off, 0, parity, slot);
     }
     __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
-        if (hash_find<W>(lookup, c) < 0) record(acc, c, a.diag, parity, slot);
+        if (hash_find<W>(lookup, c) < 0) record(acc, c, a.diag, 1, parity, slot);
     }
     __device__ __forceinline__ void reduce(Acc&) const {}
     __device__ __forceinline__ void finish(Acc&, int64_t, const Key<W>&) const {}
@@ -154,6 +157,26 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
     }
     QMBX_LAUNCH_CHECK(EMIT ? "find_relative emission pass" : "find_relative histogram pass");
     return QMBX_OK;
+}
+
+// Replace every emitted record's (slot | part << 62 | parity << 63, row) by
+// its rank key (~weight bits, ~order): the reference's exact FP64 weight and
+// its visiting order (term index, then row).  Records of zero weight (the
+// reference drops them) get the all-ones weight key, which sorts after every
+// other record, and are counted in *n_zero.
+__global__ void rank_records_kernel(uint64_t* __restrict__ rank, int64_t n, PartView off, PartView diag,
+                                    const double2* __restrict__ psi, int64_t n_i, unsigned long long* __restrict__ n_zero) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t info = rank[2 * i], row = rank[2 * i + 1];
+    const int64_t slot = (int64_t)(info & ((1ull << 62) - 1));
+    const bool in_diag = (info >> 62) & 1;
+    const int parity = (int)(info >> 63);
+    const double w = exact_weight(__ldg((in_diag ? diag.coef : off.coef) + slot), __ldg(psi + row), parity);
+    const uint64_t order = (uint64_t)__ldg((in_diag ? diag.orig : off.orig) + slot) * (uint64_t)n_i + row;
+    if (w == 0.0) atomicAdd(n_zero, 1ull);
+    rank[2 * i] = w == 0.0 ? ~0ull : ~(uint64_t)__double_as_longlong(w);
+    rank[2 * i + 1] = ~order;
 }
 
 // Gather the keys of the first `keep` ranked records.
@@ -224,6 +247,7 @@ struct FindLayout {
     double2* psi_s;         // and its amplitude
     unsigned long long* hist;
     unsigned long long* n_emit;
+    unsigned long long* n_zero;  // emitted records of zero exact weight
     int* overflow;
     uint64_t* sel_keys;
     RowSet final_set;  // built from sel_keys through a second rowset (rows are keys here)
@@ -245,6 +269,7 @@ FindLayout<W> take_find(Arena& ws, int64_t n_i, int64_t k, int64_t n_ex, int64_t
     L.psi_s = ws.take<double2>((uint64_t)n_s);
     L.hist = ws.take<unsigned long long>(kBuckets + 1);
     L.n_emit = L.hist + kBuckets;
+    L.n_zero = ws.take<unsigned long long>(1);
     L.overflow = ws.take<int>(1);
     int64_t kk = k > 0 ? k : 1;
     L.sel_keys = ws.take<uint64_t>((uint64_t)kk * W);
@@ -398,10 +423,19 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     }
     if (n_emit == 0) return QMBX_OK;
     const int64_t e = (int64_t)n_emit;
+    QMBX_CUDA_TRY(cudaMemsetAsync(L.n_zero, 0, sizeof(unsigned long long), s));
+    QMBX_KERNEL(kGroupSelect, s, rank_records_kernel<<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, e, r.off, r.diag, r.psi, a.n_i, L.n_zero));
+    QMBX_LAUNCH_CHECK("rank_records_kernel");
     if ((st = sort_pairs<2>(L.emit_rank, nullptr, L.rank_sorted, L.rank_order, e, 16, L.rank_sort, s)) != QMBX_OK) {
         return st;
     }
-    const int64_t keep = e < k ? e : k;
+    unsigned long long n_zero = 0;
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_zero, L.n_zero, sizeof(n_zero), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    // zero-weight records sort last and are never selected
+    const int64_t valid = e - (int64_t)n_zero;
+    if (valid <= 0) return QMBX_OK;
+    const int64_t keep = valid < k ? valid : k;
     QMBX_KERNEL(kGroupSelect, s, gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
                                                                             L.sel_keys));
     QMBX_LAUNCH_CHECK("gather_selected_kernel");
