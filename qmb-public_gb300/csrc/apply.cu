@@ -522,12 +522,11 @@ struct ApplyArgs {
 };
 
 // Launch one enumeration over the unique rows of `walk`: the grouped kernel
-// (warp per row) when the walked part is large, the tiled kernel (thread per
-// row) otherwise.
+// (warp per row) or the tiled kernel (thread per row), as choose_walk says.
 template <int W, class V>
 int launch_walk(const V& v, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
     UniqueRows<W> src{walk.keys, walk.unique};
-    if (part.n >= kGroupedMinTerms) {
+    if (choose_walk(part, walk.n, false) == Walk::kGrouped) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
     } else {
         QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
@@ -619,13 +618,14 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     // (gather) with daggered terms for the forward map or forward terms
     // (conjugated) for the adjoint
     const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
-    const bool pivot = part.n >= kGroupedMinTerms && use_pivot_walk(part);
-    if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashRows& walk = scatter ? in_set : out_set;
+    const Walk kind = choose_walk(part, walk.n, true);
+    const bool pivot = kind == Walk::kPivot;
+    if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashView look = scatter ? out_set.hash() : in_set.hash();
-    // large parts without the pivot walk: the grouped kernel walks the
-    // changing terms and a tiled pass adds the diagonal ones
-    const bool grouped = !pivot && part.n >= kGroupedMinTerms;
+    // the grouped kernel walks the changing terms and a tiled pass adds the
+    // diagonal ones
+    const bool grouped = kind == Walk::kGrouped;
     PartView walk_diag = diag;
     if (grouped) walk_diag.n = 0;
     if (pivot) {
@@ -769,7 +769,7 @@ int diagonal_impl(const void* table_host, const void* table_dev, const uint8_t* 
     PartView diag = part_view(table_host, table_dev, QMBX_PART_DIAG);
     DiagonalF64<W> v{{}, diag.coef, out};
     ByteRows<W> src{configs, h->n_qubytes};
-    if (diag.n >= kGroupedMinTerms) {
+    if (choose_walk(diag, n, false) == Walk::kGrouped) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));
     } else {
         QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, none, diag));

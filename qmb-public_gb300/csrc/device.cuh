@@ -908,12 +908,20 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
 // Grid for pivot_kernel: a few resident blocks per SM, looping over work items.
 int pivot_grid();
 
-// Which walk a large term part takes: the pivot-major kernel when its
-// non-empty groups hold kPivotMeanGroup terms or more on average, the
-// grouped (warp per row) kernel otherwise.  QMBX_WALK=pivot or
-// QMBX_WALK=grouped in the environment forces one; read once per process.
+// Which kernel walks a term part over n_rows rows:
+//   pivot    parts of kGroupedMinTerms terms or more whose non-empty groups
+//            hold kPivotMeanGroup terms or more on average (when the caller
+//            has a pivot-major visitor);
+//   grouped  other parts of kGroupedMinTerms terms or more, and any part over
+//            fewer than kFewRows rows (a thread per row would leave most of
+//            the GPU idle);
+//   tiled    small parts over many rows.
+// QMBX_WALK=pivot, grouped or tiled in the environment forces a kernel
+// (read at every call; pivot falls back to grouped where it cannot serve).
 constexpr int kPivotMeanGroup = 768;
-bool use_pivot_walk(const PartView& part);
+constexpr int64_t kFewRows = 65536;
+enum class Walk { kTiled, kGrouped, kPivot };
+Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok);
 
 // Grid for grouped_kernel: enough warps for every row, at most a few waves.
 int grouped_grid(int64_t n_rows);

@@ -570,13 +570,18 @@ static int sm_count() {
 
 int pivot_grid() { return sm_count() * 4; }
 
-bool use_pivot_walk(const PartView& part) {
-    // QMBX_WALK=pivot or grouped overrides the choice (read at every call)
+Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok) {
     const char* e = getenv("QMBX_WALK");
-    if (e != nullptr && e[0] == 'p') return true;
-    if (e != nullptr && e[0] == 'g') return false;
-    // groups holding hundreds of terms amortise staging them in shared memory
-    return part.n_nonempty > 0 && part.n >= (int64_t)kPivotMeanGroup * part.n_nonempty;
+    const char f = e != nullptr ? e[0] : 0;
+    if (part.n == 0 || f == 't') return Walk::kTiled;
+    if (f == 'p') return pivot_ok ? Walk::kPivot : Walk::kGrouped;
+    if (f == 'g') return Walk::kGrouped;
+    if (part.n >= kGroupedMinTerms) {
+        // groups holding hundreds of terms amortise staging them in shared memory
+        const bool big_groups = part.n_nonempty > 0 && part.n >= (int64_t)kPivotMeanGroup * part.n_nonempty;
+        return pivot_ok && big_groups ? Walk::kPivot : Walk::kGrouped;
+    }
+    return n_rows < kFewRows ? Walk::kGrouped : Walk::kTiled;
 }
 
 int grouped_grid(int64_t n_rows) {

@@ -142,9 +142,10 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
     v.a = r;
     v.lookup = r.excl;
     KeyRows<W> src{keys_i};
-    if (r.off.n >= kGroupedMinTerms && !use_pivot_walk(r.off)) {
+    const Walk kind = choose_walk(r.off, n_i, true);
+    if (kind == Walk::kGrouped) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
-    } else if (r.off.n >= kGroupedMinTerms) {
+    } else if (kind == Walk::kPivot) {
         // pivot-major walk of the changing terms, then the diagonal terms tiled
         QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off));
         if (r.diag.n > 0) {
@@ -574,7 +575,7 @@ int single_impl(const void* table_host, const void* table_dev, const uint8_t* co
     none.n = 0;
     SingleVisitor<W> v{{}, L.set.hash(), L.kf, off.orig, out, h->n_qubytes};
     KeyRows<W> src{L.set.keys};
-    if (off.n >= kGroupedMinTerms) {
+    if (choose_walk(off, n, false) == Walk::kGrouped) {
         QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n), kThreads, 0, s>>>(v, src, nullptr, n, off, none));
     } else {
         QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(v, src, nullptr, n, off, none));

@@ -2,7 +2,9 @@
 
 Tolerances: FP64 apply_within / diagonal_term agree to 1e-12 of the absolute
 sum of the contributions to each amplitude (summation order differs from the
-reference's); find_relative rows are compared byte for byte.
+reference's); find_relative rows are compared byte for byte.  The main cases
+run with each walk kernel (tiled, grouped, pivot) forced in turn, besides the
+automatic choice.
 """
 
 from __future__ import annotations
@@ -36,8 +38,19 @@ def dev(x, device):
     return torch.from_numpy(np.ascontiguousarray(x)).to(device)
 
 
+WALKS = ["auto", "tiled", "grouped", "pivot"]
+
+
+@pytest.fixture(params=WALKS)
+def walk(request, monkeypatch):
+    """Every walk kernel on every case: the automatic choice, or one forced through QMBX_WALK."""
+    if request.param != "auto":
+        monkeypatch.setenv("QMBX_WALK", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_apply_within_matches_reference(case, cuda_device):
+def test_apply_within_matches_reference(case, walk, cuda_device):
     g = golden(case)
     ham = ham_of(g)
     got = ham.apply_within(dev(g["configs_i"], cuda_device), dev(g["psi_i"], cuda_device),
@@ -54,14 +67,14 @@ def test_apply_within_matches_reference(case, cuda_device):
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_diagonal_term_matches_reference(case, cuda_device):
+def test_diagonal_term_matches_reference(case, walk, cuda_device):
     g = golden(case)
     got = ham_of(g).diagonal_term(dev(g["diag_configs"], cuda_device)).cpu().numpy()
     np.testing.assert_allclose(got, g["diag"], rtol=0, atol=RTOL_F64 * np.abs(g["coef"]).sum())
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_find_relative_matches_reference(case, cuda_device):
+def test_find_relative_matches_reference(case, walk, cuda_device):
     g = golden(case)
     ham = ham_of(g)
     pc = int(g["particle_cut"])
@@ -112,7 +125,7 @@ def test_adjoint_against_dense_matrix(cuda_device):
 
 
 @pytest.mark.parametrize("case", ["ab_initio_6", "ab_initio_10_complex", "random_terms_fermi", "ising_4x4"])
-def test_compensated_fp32_tracks_fp64(case, cuda_device):
+def test_compensated_fp32_tracks_fp64(case, walk, cuda_device):
     g = golden(case)
     ham = ham_of(g)
     ci, cj = dev(g["configs_i"], cuda_device), dev(g["configs_j"], cuda_device)
@@ -127,7 +140,7 @@ def test_compensated_fp32_tracks_fp64(case, cuda_device):
     assert np.all(np.abs(plain - exact) <= 2e-7 * (scale + np.abs(exact)))
 
 
-def test_single_relative_matches_oracle(cuda_device):
+def test_single_relative_matches_oracle(walk, cuda_device):
     for case in ("ab_initio_10_complex", "random_terms_fermi", "random_terms_bose2", "ising_4x4"):
         g = golden(case)
         ham = ham_of(g)
