@@ -720,13 +720,21 @@ __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, cons
 #pragma unroll 1
         while (cur.next(g, c, pv)) walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
     } else {
-        // small groups: lane k takes every 32nd group of the sequence
+        // small groups: the cursor deals 32 groups to the lanes, one each,
+        // then every lane walks its group (all 32 at once)
         int k = 0;
+        int64_t mine = -1;
 #pragma unroll 1
         while (cur.next(g, c, pv)) {
-            if (k == lane) walk_group_serial<W, DIAG>(v, acc, c, pv, g);
-            k = (k + 1) & 31;
+            if (k == lane) mine = g;
+            if (++k == 32) {
+                walk_group_serial<W, DIAG>(v, acc, c, pv, mine);
+                __syncwarp();
+                mine = -1;
+                k = 0;
+            }
         }
+        if (mine >= 0) walk_group_serial<W, DIAG>(v, acc, c, pv, mine);
         __syncwarp();
     }
 }
