@@ -1001,18 +1001,16 @@ int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s
 // A de-duplicated row set without sorting: every row's key is inserted in an
 // open-addressing hash set whose entries name the first (lowest) row holding
 // that key.  first[i] is that row for every row i; unique[0 .. *count) lists
-// the first rows in row order.  Lookups (hash()) return first rows, so
-// per-key data is stored at the first row's index.
+// the first rows (in no particular order: the walks treat rows
+// independently).  Lookups (hash()) return first rows, so per-key data is
+// stored at the first row's index.
 struct HashRows {
     uint64_t* keys;     // n x W, row order
     uint64_t* slots;
     uint64_t slot_mask;
     int32_t* first;     // n
-    int32_t* unique;    // n (first *count valid)
-    int32_t* head;      // n: 1 where first[i] == i
-    int32_t* pos;       // n
+    int32_t* unique;    // n (first *count valid, in no particular order)
     int* count;
-    int32_t* scan;      // scan scratch
     uint32_t* bloom;    // filter over the keys (bloom_words_for(n) words), or NULL
     uint32_t bloom_words;
     int64_t n;

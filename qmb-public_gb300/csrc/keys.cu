@@ -436,11 +436,15 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
 // sequence.
 template <int W>
 __global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint64_t* __restrict__ slots,
-                                       uint64_t mask) {
+                                       uint64_t mask, uint32_t* __restrict__ bloom, uint32_t bloom_mask) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const Key<W> k = load_key<W>(keys, r);
     const uint64_t hv = key_hash<W>(k);
+    if (bloom != nullptr) {
+        const uint64_t f = bloom_mix(hv);
+        atomicOr(bloom + bloom_word(f, bloom_mask), bloom_bits(f));
+    }
     uint64_t i = hash_home(hv, hash_shift(mask + 1));
     uint32_t* w = reinterpret_cast<uint32_t*>(slots);
     for (uint64_t probe = 0; probe <= mask; ++probe) {
@@ -461,33 +465,27 @@ __global__ void hashrows_insert_kernel(const uint64_t* __restrict__ keys, int64_
     }
 }
 
-// Set the filter bits of every row's key.
-template <int W>
-__global__ void bloom_insert_kernel(const uint64_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ bloom,
-                                    uint32_t mask) {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    const uint64_t f = bloom_mix(key_hash<W>(load_key<W>(keys, r)));
-    atomicOr(bloom + bloom_word(f, mask), bloom_bits(f));
-}
-
-// first[r] = lowest row with row r's key; head[r] = (first[r] == r).
+// first[r] = lowest row with row r's key; every such first row is listed in
+// unique[0 .. *count) (in no particular order: a warp reserves its places
+// with one atomic).
 template <int W>
 __global__ void hashrows_resolve_kernel(const uint64_t* __restrict__ keys, int64_t n, HashView h,
-                                        int32_t* __restrict__ first, int32_t* __restrict__ head) {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    int64_t f = hash_find<W>(h, load_key<W>(keys, r));
-    first[r] = (int32_t)f;
-    head[r] = f == r ? 1 : 0;
-}
-
-__global__ void hashrows_compact_kernel(const int32_t* __restrict__ head, const int32_t* __restrict__ pos, int64_t n,
-                                        int32_t* __restrict__ unique, int* __restrict__ count) {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    if (head[r]) unique[pos[r]] = (int32_t)r;
-    if (r == n - 1) *count = pos[r] + head[r];
+                                        int32_t* __restrict__ first, int32_t* __restrict__ unique,
+                                        int* __restrict__ count) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = r < n;
+    int64_t f = -1;
+    if (live) {
+        f = hash_find<W>(h, load_key<W>(keys, r));
+        first[r] = (int32_t)f;
+    }
+    const bool head = live && f == r;
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    const int lane = threadIdx.x & 31;
+    int at = 0;
+    if (lane == 0 && m) at = atomicAdd(count, __popc(m));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (head) unique[at + __popc(m & ((1u << lane) - 1u))] = (int32_t)r;
 }
 
 template <int W>
@@ -502,10 +500,7 @@ HashRows take_hashrows(Arena& ws, int64_t n) {
     out.slot_mask = slots - 1;
     out.first = ws.take<int32_t>(cap);
     out.unique = ws.take<int32_t>(cap);
-    out.head = ws.take<int32_t>(cap);
-    out.pos = ws.take<int32_t>(cap);
     out.count = ws.take<int>(1);
-    out.scan = ws.take<int32_t>((uint64_t)scan_scratch((int64_t)cap));
     out.bloom_words = bloom_words_for(n);
     out.bloom = out.bloom_words ? ws.take<uint32_t>(out.bloom_words) : nullptr;
     return out;
@@ -515,23 +510,17 @@ template <int W>
 int build_hashrows(const uint8_t* rows, int nq, HashRows& out, cudaStream_t s) {
     const int64_t n = out.n;
     QMBX_CUDA_TRY(cudaMemsetAsync(out.slots, 0xff, (out.slot_mask + 1) * sizeof(uint64_t), s));
-    if (n == 0) {
-        QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
-        QMBX_LAUNCH_CHECK("set_int_kernel");
-        return QMBX_OK;
-    }
+    QMBX_CUDA_TRY(cudaMemsetAsync(out.count, 0, sizeof(int), s));
+    if (n == 0) return QMBX_OK;
     int st;
     if ((st = pack_rows<W>(rows, n, nq, out.keys, s)) != QMBX_OK) return st;
     const unsigned grid = grid_for(n, kThreads);
-    if (out.bloom_words) {
-        // complete before the first lookup (the resolve pass below)
-        QMBX_CUDA_TRY(cudaMemsetAsync(out.bloom, 0, (size_t)out.bloom_words * sizeof(uint32_t), s));
-        QMBX_KERNEL(kGroupKeys, s, bloom_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.bloom, out.bloom_words - 1));
-    }
-    QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.slots, out.slot_mask));
-    QMBX_KERNEL(kGroupKeys, s, hashrows_resolve_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.hash(), out.first, out.head));
-    if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.scan, s)) != QMBX_OK) return st;
-    QMBX_KERNEL(kGroupKeys, s, hashrows_compact_kernel<<<grid, kThreads, 0, s>>>(out.head, out.pos, n, out.unique, out.count));
+    // the filter (when the set has one) is complete before the first lookup (the resolve pass)
+    if (out.bloom_words) QMBX_CUDA_TRY(cudaMemsetAsync(out.bloom, 0, (size_t)out.bloom_words * sizeof(uint32_t), s));
+    QMBX_KERNEL(kGroupKeys, s, hashrows_insert_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.slots, out.slot_mask,
+                                                                  out.bloom_words ? out.bloom : nullptr,
+                                                                  out.bloom_words ? out.bloom_words - 1 : 0));
+    QMBX_KERNEL(kGroupKeys, s, hashrows_resolve_kernel<W><<<grid, kThreads, 0, s>>>(out.keys, n, out.hash(), out.first, out.unique, out.count));
     QMBX_LAUNCH_CHECK("build_hashrows");
     return QMBX_OK;
 }
