@@ -535,14 +535,19 @@ int launch_walk(const V& v, const HashRows& walk, const PartView& part, const Pa
     return QMBX_OK;
 }
 
-// Tiled pass over the diagonal terms of every walked row (adds into res).
+// Pass over the diagonal terms of every walked row (adds into res): grouped
+// or tiled, as choose_walk says.
 template <int W, class D>
 int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
     if (diag.n == 0) return QMBX_OK;
     UniqueRows<W> src{walk.keys, walk.unique};
     PartView none = part;
     none.n = 0;
-    QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+    if (choose_walk(diag, walk.n, false) == Walk::kGrouped) {
+        QMBX_KERNEL(kGroupDiagonal, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+    } else {
+        QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+    }
     QMBX_LAUNCH_CHECK("apply_within diagonal pass");
     return QMBX_OK;
 }

@@ -920,14 +920,17 @@ int pivot_grid();
 //   pivot    parts of kGroupedMinTerms terms or more whose non-empty groups
 //            hold kPivotMeanGroup terms or more on average (when the caller
 //            has a pivot-major visitor);
-//   grouped  other parts of kGroupedMinTerms terms or more, and any part over
-//            fewer than kFewRows rows (a thread per row would leave most of
-//            the GPU idle);
-//   tiled    small parts over many rows.
+//   grouped  other parts of kGroupedMinTerms terms or more, and smaller parts
+//            over fewer than kFewRows rows (kFewWideRows when the part's
+//            groups are large), where a thread per row would leave most of
+//            the GPU idle;
+//   tiled    small parts over more rows (e.g. the diagonal parts, whose
+//            groups hold one term or two, over 20,000 rows).
 // QMBX_WALK=pivot, grouped or tiled in the environment forces a kernel
 // (read at every call; pivot falls back to grouped where it cannot serve).
 constexpr int kPivotMeanGroup = 768;
-constexpr int64_t kFewRows = 65536;
+constexpr int64_t kFewRows = 8192;
+constexpr int64_t kFewWideRows = 65536;
 enum class Walk { kTiled, kGrouped, kPivot };
 Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok);
 

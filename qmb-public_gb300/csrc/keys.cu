@@ -570,7 +570,7 @@ Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok) {
         const bool big_groups = part.n_nonempty > 0 && part.n >= (int64_t)kPivotMeanGroup * part.n_nonempty;
         return pivot_ok && big_groups ? Walk::kPivot : Walk::kGrouped;
     }
-    return n_rows < kFewRows ? Walk::kGrouped : Walk::kTiled;
+    return n_rows < (part.wide ? kFewWideRows : kFewRows) ? Walk::kGrouped : Walk::kTiled;
 }
 
 int grouped_grid(int64_t n_rows) {

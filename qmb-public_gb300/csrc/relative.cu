@@ -151,7 +151,11 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
         if (r.diag.n > 0) {
             PartView none = r.off;
             none.n = 0;
-            QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, none, r.diag));
+            if (choose_walk(r.diag, n_i, false) == Walk::kGrouped) {
+                QMBX_KERNEL(kGroupDiagonal, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, none, r.diag));
+            } else {
+                QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, none, r.diag));
+            }
         }
     } else {
         QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(n_i, kThreads), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
