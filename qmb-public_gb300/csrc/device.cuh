@@ -928,7 +928,7 @@ int pivot_grid();
 //            groups hold one term or two, over 20,000 rows).
 // QMBX_WALK=pivot, grouped or tiled in the environment forces a kernel
 // (read at every call; pivot falls back to grouped where it cannot serve).
-constexpr int kPivotMeanGroup = 768;
+constexpr int kPivotMeanGroup = 300;
 constexpr int64_t kFewRows = 8192;
 constexpr int64_t kFewWideRows = 65536;
 enum class Walk { kTiled, kGrouped, kPivot };
