@@ -198,3 +198,35 @@ def test_errors_are_raised_not_trapped(cuda_device):
         ham.apply_within(c.cpu(), torch.from_numpy(g["psi_i"][:10]), c.cpu())
     # the context is still usable
     assert ham.diagonal_term(c).shape == (10,)
+
+
+@pytest.mark.parametrize("case", ["hubbard_3x2", "ab_initio_6"])
+def test_single_relative_frequencies_follow_coefficients(case, cuda_device):
+    """The reference's sampling law (qmb/_hamiltonian_cuda.cu:854-866): a neighbour is drawn with
+    probability sum |c_t| over the terms that lead to it, over sum |c_t| of all candidates; a
+    chi-squared test over 4,000 seeds for one row."""
+    scipy_stats = pytest.importorskip("scipy.stats")
+    g = golden(case)
+    ham = ham_of(g)
+    pc = int(g["particle_cut"])
+    row = g["configs_i"][:1]
+    weight = {}
+    for t in range(g["site"].shape[0]):
+        ok, _, out = oracle.apply_term(g["site"][t], g["kind"][t], row[0], pc)
+        if ok and not np.array_equal(out, row[0]):
+            key = bytes(out)
+            weight[key] = weight.get(key, 0.0) + float(np.hypot(*g["coef"][t]))
+    weight = {k: w for k, w in weight.items() if w > 0}
+    assert len(weight) >= 4
+    keys = sorted(weight)
+    total = sum(weight.values())
+    counts = dict.fromkeys(keys, 0)
+    c = dev(row, cuda_device)
+    n = 4000
+    for seed in range(n):
+        got = bytes(ham.single_relative_seeded(c, 7919 * seed + 1).cpu().numpy()[0])
+        counts[got] += 1
+    observed = np.array([counts[k] for k in keys], dtype=np.float64)
+    expected = np.array([n * weight[k] / total for k in keys])
+    stat = float(((observed - expected) ** 2 / expected).sum())
+    assert scipy_stats.chi2.sf(stat, len(keys) - 1) > 1e-4, (stat, len(keys))
