@@ -56,6 +56,12 @@ struct CompSum {
         two_sum(s, x, s, e);
         c = __fadd_rn(c, e);
     }
+    // a value split in a leading part and a tail (a coefficient's hi/lo pair)
+    __device__ __forceinline__ void add2(float hi, float lo) {
+        float e;
+        two_sum(s, hi, s, e);
+        c = __fadd_rn(c, __fadd_rn(e, lo));
+    }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
     // Combine the lanes' pairs: two-sum of the leading parts, plain sum of the tails.
     __device__ __forceinline__ void warp_reduce() {
@@ -69,6 +75,17 @@ struct CompSum {
         }
     }
 };
+
+// A diagonal coefficient (hi/lo split) with sign (-1)^parity and optional
+// conjugation, added to the compensated sums (dre, dim): FP32 work, so that
+// the divergent per-term adds of a walk do not queue on the FP64 pipe.
+template <bool CONJ>
+__device__ __forceinline__ void comp_diag_add(CompSum& dre, CompSum& dim, float4 cf, int parity) {
+    const float sg = parity ? -1.f : 1.f;
+    const float ih = CONJ ? -cf.z : cf.z, il = CONJ ? -cf.w : cf.w;
+    dre.add2(sg * cf.x, sg * cf.y);
+    dim.add2(sg * ih, sg * il);
+}
 
 // coef (hi/lo split, sign already folded) times psi, added to (re, im) with
 // sign (-1)^parity and optional conjugation of the coefficient.
@@ -182,18 +199,18 @@ struct GatherF32C : VisitorBase {
     HashView lookup;
     const float2* val;
     const float4* coef32;
-    const double2* dcoef;
+    const float4* dcoef32;   // diagonal part, hi/lo FP32
     int include_diag;
     const int32_t* unique;
     double2* res;
     struct Acc {
-        CompSum re, im;
-        double dre, dim;
+        CompSum re, im, dre, dim;
     };
     __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const {
         a.re.zero();
         a.im.zero();
-        a.dre = a.dim = 0.0;
+        a.dre.zero();
+        a.dim.zero();
     }
     static constexpr bool kBatched = true;
     static constexpr bool kProbe = true;
@@ -215,25 +232,23 @@ struct GatherF32C : VisitorBase {
         if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
-        double2 cf = __ldg(dcoef + slot);
-        double ci = CONJ ? -cf.y : cf.y;
-        a.dre += parity ? -cf.x : cf.x;
-        a.dim += parity ? -ci : ci;
+        comp_diag_add<CONJ>(a.dre, a.dim, __ldg(dcoef32 + slot), parity);
     }
     __device__ __forceinline__ void reduce(Acc& a) const {
         a.re.warp_reduce();
         a.im.warp_reduce();
-        a.dre = warp_sum(a.dre);
-        a.dim = warp_sum(a.dim);
+        a.dre.warp_reduce();
+        a.dim.warp_reduce();
     }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         double re = a.re.value(), im = a.im.value();
-        if (include_diag && (a.dre != 0.0 || a.dim != 0.0)) {
+        const double dre = a.dre.value(), dim = a.dim.value();
+        if (include_diag && (dre != 0.0 || dim != 0.0)) {
             int64_t pos = hash_find<W>(lookup, c);
             if (pos >= 0) {
                 float2 p = __ldg(val + pos);
-                re += a.dre * (double)p.x - a.dim * (double)p.y;
-                im += a.dre * (double)p.y + a.dim * (double)p.x;
+                re += dre * (double)p.x - dim * (double)p.y;
+                im += dre * (double)p.y + dim * (double)p.x;
             }
         }
         res[__ldg(unique + u)] = make_double2(re, im);
@@ -279,12 +294,14 @@ struct Scatter : VisitorBase {
     const int32_t* unique;  // walk index -> first row of the walked key
     const double2* coef;    // walked part, FP64
     const float4* coef32;   // walked part, hi/lo FP32
-    const double2* dcoef;   // diagonal part
+    const double2* dcoef;   // diagonal part (FP64 path)
+    const float4* dcoef32;  // diagonal part, hi/lo FP32 (F32 path)
     int include_diag;
     double2* acc;           // per unique output-side key
     struct Acc {
         double2 p;
-        double dre, dim;
+        double dre, dim;    // FP64 path
+        CompSum fre, fim;   // F32 path
     };
     __device__ __forceinline__ void init(Acc& a, int64_t u, const Key<W>&, int*) const {
         const int64_t row = __ldg(unique + u);
@@ -295,6 +312,8 @@ struct Scatter : VisitorBase {
             a.p = __ldg(static_cast<const double2*>(val) + row);
         }
         a.dre = a.dim = 0.0;
+        a.fre.zero();
+        a.fim.zero();
     }
     static constexpr bool kBatched = true;
     static constexpr bool kProbe = true;
@@ -344,21 +363,31 @@ struct Scatter : VisitorBase {
         if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
-        double2 cf = __ldg(dcoef + slot);
-        double ci = CONJ ? -cf.y : cf.y;
-        a.dre += parity ? -cf.x : cf.x;
-        a.dim += parity ? -ci : ci;
+        if (F32) {
+            comp_diag_add<CONJ>(a.fre, a.fim, __ldg(dcoef32 + slot), parity);
+        } else {
+            double2 cf = __ldg(dcoef + slot);
+            double ci = CONJ ? -cf.y : cf.y;
+            a.dre += parity ? -cf.x : cf.x;
+            a.dim += parity ? -ci : ci;
+        }
     }
     __device__ __forceinline__ void reduce(Acc& a) const {
-        a.dre = warp_sum(a.dre);
-        a.dim = warp_sum(a.dim);
+        if (F32) {
+            a.fre.warp_reduce();
+            a.fim.warp_reduce();
+        } else {
+            a.dre = warp_sum(a.dre);
+            a.dim = warp_sum(a.dim);
+        }
     }
     __device__ __forceinline__ void finish(Acc& a, int64_t, const Key<W>& c) const {
-        if (!include_diag || (a.dre == 0.0 && a.dim == 0.0)) return;
+        const double dre = F32 ? a.fre.value() : a.dre, dim = F32 ? a.fim.value() : a.dim;
+        if (!include_diag || (dre == 0.0 && dim == 0.0)) return;
         int64_t u = hash_find<W>(lookup, c);
         if (u < 0) return;
-        atomicAdd(&acc[u].x, a.dre * a.p.x - a.dim * a.p.y);
-        atomicAdd(&acc[u].y, a.dre * a.p.y + a.dim * a.p.x);
+        atomicAdd(&acc[u].x, dre * a.p.x - dim * a.p.y);
+        atomicAdd(&acc[u].y, dre * a.p.y + dim * a.p.x);
     }
 };
 
@@ -428,24 +457,43 @@ struct DiagAdd : VisitorBase {
     HashView lookup;
     const void* val;
     const int32_t* unique;
-    const double2* dcoef;
+    const double2* dcoef;    // FP64 path
+    const float4* dcoef32;   // F32 path (hi/lo)
     double2* res;
     struct Acc {
-        double dre, dim;
+        double dre, dim;     // FP64 path
+        CompSum fre, fim;    // F32 path
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.dre = a.dim = 0.0; }
+    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const {
+        a.dre = a.dim = 0.0;
+        a.fre.zero();
+        a.fim.zero();
+    }
     __device__ __forceinline__ void visit(Acc&, const Key<W>&, const Key<W>&, int, int64_t) const {}
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
-        const double2 cf = __ldg(dcoef + slot);
-        const double ci = CONJ ? -cf.y : cf.y;
-        a.dre += parity ? -cf.x : cf.x;
-        a.dim += parity ? -ci : ci;
+        if (F32) {
+            comp_diag_add<CONJ>(a.fre, a.fim, __ldg(dcoef32 + slot), parity);
+        } else {
+            const double2 cf = __ldg(dcoef + slot);
+            const double ci = CONJ ? -cf.y : cf.y;
+            a.dre += parity ? -cf.x : cf.x;
+            a.dim += parity ? -ci : ci;
+        }
     }
     __device__ __forceinline__ void reduce(Acc& a) const {
-        a.dre = warp_sum(a.dre);
-        a.dim = warp_sum(a.dim);
+        if (F32) {
+            a.fre.warp_reduce();
+            a.fim.warp_reduce();
+        } else {
+            a.dre = warp_sum(a.dre);
+            a.dim = warp_sum(a.dim);
+        }
     }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
+        if (F32) {
+            a.dre = a.fre.value();
+            a.dim = a.fim.value();
+        }
         if (a.dre == 0.0 && a.dim == 0.0) return;
         const int64_t pos = hash_find<W>(lookup, c);
         if (pos < 0) return;
@@ -637,7 +685,7 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
 #define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
     {                                                                                                            \
         PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res};             \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, res};                           \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res};                           \
         st = launch_pivot<W>(v, dv, walk, part, diag, s);                                                        \
     }
         const bool f32 = a.prec == Prec::F32C;
@@ -658,18 +706,18 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     } else if (scatter) {
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
-                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
+                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, 1, res};
+                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         } else {
             if (a.adjoint) {
-                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, include_diag, res};
+                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
@@ -684,10 +732,10 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
             }
         } else {
             if (a.adjoint) {
-                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
+                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef, a.include_diag, walk.unique, res};
+                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res};
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
@@ -697,7 +745,7 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         const bool f32 = a.prec == Prec::F32C;
 #define QMBX_DIAG_CASE(CONJ, F32, SCATTER)                                              \
     {                                                                                   \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, res};  \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res};  \
         st = launch_diag<W>(dv, walk, part, diag, s);                                   \
     }
         if (scatter) {
