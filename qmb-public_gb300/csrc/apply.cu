@@ -548,7 +548,7 @@ __global__ void sum_repeats_kernel(const T* __restrict__ psi, const int32_t* __r
 }
 
 // ---------------------------------------------------------------------------
-// host drivers
+// host side: workspace layout and kernel launches
 // ---------------------------------------------------------------------------
 
 enum class Prec { F64, F32C };
