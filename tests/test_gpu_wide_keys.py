@@ -5,8 +5,10 @@ cases cover the three- and four-word instantiations of every kernel: a
 Fermi-Hubbard lattice of 160 and 256 spin orbitals (n_qubytes 20 and 32) and
 random operator strings over 256 sites with fermions and hard-core bosons.
 Targets include the sources' neighbours, so that lookups hit.  Every walk
-kernel is forced in turn.  Tolerances as in the golden parity tests: FP64 to
-1e-12 of the per-amplitude absolute sum, find_relative byte for byte.
+kernel is forced in turn.  Tolerances as in the golden parity tests: FP64 and
+compensated FP32 (same FP32 amplitudes) to 1e-12 of the per-amplitude
+absolute sum, the adjoint through <g, H psi> = <H^dagger g, psi>,
+find_relative byte for byte.
 """
 
 from __future__ import annotations
@@ -78,6 +80,15 @@ def test_wide_keys_against_oracle(case, walk, cuda_device):
     got = ham.apply_within(dev(rows), dev(psi), dev(targets)).cpu().numpy()
     assert np.count_nonzero(want) > 50, name
     assert np.all(np.abs(got - want) <= 1e-12 * scale + 1e-30), name
+
+    # compensated FP32 on the same FP32 amplitudes, and the adjoint against the forward map
+    psi32 = psi.astype(np.complex64)
+    want32 = oracle.apply_within(site, kind, coef, rows, psi32.astype(np.complex128), targets, pc)
+    got32 = ham.apply_within_compensated(dev(rows), dev(psi32), dev(targets)).cpu().numpy()
+    assert np.all(np.abs(got32 - want32) <= 1e-12 * scale + 1e-30), name
+    g = rng.standard_normal(targets.shape[0]) + 1j * rng.standard_normal(targets.shape[0])
+    adj = ham.apply_within_adjoint(dev(rows), dev(g), dev(targets)).cpu().numpy()
+    assert abs(np.vdot(g, got) - np.vdot(adj, psi)) <= 1e-11 * (np.abs(g) @ scale + 1), name
 
     diag = ham.diagonal_term(dev(targets[:200])).cpu().numpy()
     want_diag = oracle.diagonal_term(site, kind, coef, targets[:200], pc)
