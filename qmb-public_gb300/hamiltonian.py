@@ -129,7 +129,9 @@ class Hamiltonian:
         if table is None:
             with torch.cuda.device(device):
                 table = _Table(self.site, self.kind, self.coef, n_qubytes, self.particle_cut, device)
-            self._tables = {k: v for k, v in self._tables.items() if k[0] != device.index}
+            # tables of this device compiled from other term tensors (or older
+            # versions of them) are stale; those for other row widths are kept
+            self._tables = {k: v for k, v in self._tables.items() if k[0] != device.index or k[2:] == key[2:]}
             self._tables[key] = table
         return table
 
