@@ -23,6 +23,7 @@
 //                  key of its candidates in registers.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <vector>
 
 #include "device.cuh"
@@ -165,12 +166,15 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
 }
 
 // Replace every emitted record's (slot | part << 62 | parity << 63, row) by
-// its rank key (~weight bits, ~order): the reference's exact FP64 weight and
-// its visiting order (term index, then row).  Records of zero weight (the
-// reference drops them) get the all-ones weight key, which sorts after every
-// other record, and are counted in *n_zero.
+// its rank key (~weight bits, ~order << order_shift): the reference's exact
+// FP64 weight and its visiting order (term index, then row).  Orders are
+// below 2^(64 - order_shift), so the key's leading 8 + (64 - order_shift) / 8
+// bytes decide it and the radix sort skips the rest.  Records of zero weight
+// (the reference drops them) get the all-ones weight key, which sorts after
+// every other record, and are counted in *n_zero.
 __global__ void rank_records_kernel(uint64_t* __restrict__ rank, int64_t n, PartView off, PartView diag,
-                                    const double2* __restrict__ psi, int64_t n_i, unsigned long long* __restrict__ n_zero) {
+                                    const double2* __restrict__ psi, int64_t n_i, int order_shift,
+                                    unsigned long long* __restrict__ n_zero) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t info = rank[2 * i], row = rank[2 * i + 1];
@@ -181,7 +185,7 @@ __global__ void rank_records_kernel(uint64_t* __restrict__ rank, int64_t n, Part
     const uint64_t order = (uint64_t)__ldg((in_diag ? diag.orig : off.orig) + slot) * (uint64_t)n_i + row;
     if (w == 0.0) atomicAdd(n_zero, 1ull);
     rank[2 * i] = w == 0.0 ? ~0ull : ~(uint64_t)__double_as_longlong(w);
-    rank[2 * i + 1] = ~order;
+    rank[2 * i + 1] = (~order) << order_shift;
 }
 
 // Gather the keys of the first `keep` ranked records.
@@ -429,9 +433,16 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     if (n_emit == 0) return QMBX_OK;
     const int64_t e = (int64_t)n_emit;
     QMBX_CUDA_TRY(cudaMemsetAsync(L.n_zero, 0, sizeof(unsigned long long), s));
-    QMBX_KERNEL(kGroupSelect, s, rank_records_kernel<<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, e, r.off, r.diag, r.psi, a.n_i, L.n_zero));
+    // bytes of the visiting order (term index * n_i + row < n_terms * n_i)
+    int order_bytes = 1;
+    {
+        const double span = (double)(h->n_terms > 0 ? h->n_terms : 1) * (double)a.n_i;
+        while (order_bytes < 8 && span > std::ldexp(1.0, 8 * order_bytes)) ++order_bytes;
+    }
+    const int order_shift = 64 - 8 * order_bytes;
+    QMBX_KERNEL(kGroupSelect, s, rank_records_kernel<<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, e, r.off, r.diag, r.psi, a.n_i, order_shift, L.n_zero));
     QMBX_LAUNCH_CHECK("rank_records_kernel");
-    if ((st = sort_pairs<2>(L.emit_rank, nullptr, L.rank_sorted, L.rank_order, e, 16, L.rank_sort, s)) != QMBX_OK) {
+    if ((st = sort_pairs<2>(L.emit_rank, nullptr, L.rank_sorted, L.rank_order, e, 8 + order_bytes, L.rank_sort, s)) != QMBX_OK) {
         return st;
     }
     unsigned long long n_zero = 0;
