@@ -105,3 +105,21 @@ def test_fcidump_gzip_and_bad_line(tmp_path):
     bad.write_text(" &FCI NORB=2,NELEC=2,MS2=0,\n &END\n 1.0 1 2 1 0\n")
     with pytest.raises(ValueError):
         terms.read_fcidump(str(bad))
+
+
+def test_hamiltonian_rejects_bad_inputs_on_the_host():
+    from qmb_gb300 import Hamiltonian
+
+    site, kind, coef = terms.integral_hamiltonian_tables(3, seed=1)
+    ham = Hamiltonian((site, kind, coef), kind="fermi")
+    rows = torch.from_numpy(terms.all_determinants(3, 1, 1))
+    psi = torch.ones(rows.shape[0], dtype=torch.complex128)
+    with pytest.raises(RuntimeError, match="uint8"):
+        ham.apply_within(rows.to(torch.int32), psi, rows)
+    with pytest.raises(RuntimeError, match="2D"):
+        ham.diagonal_term(rows.flatten())
+    # the engine has no CPU path: CPU tensors are refused, not computed some other way
+    with pytest.raises(RuntimeError, match="CUDA"):
+        ham.apply_within(rows, psi, rows)
+    with pytest.raises(ValueError):
+        Hamiltonian((site, kind, coef), kind="bose3")
