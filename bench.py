@@ -7,16 +7,27 @@ determinants with 5 alpha + 5 beta electrons, complex N(0,1) amplitudes.
 
 One step is the FP32-compensated apply_within forward (configs_i ->
 configs_j) followed by its adjoint (configs_j -> configs_i), i.e. the work of
-one energy-gradient evaluation.  The metric is term applications per second,
-T * (N_i + N_j) per step (the reference's thread grid is T * N_i for a
-forward application).  The same line reports the FP64 path, find_relative
-(top 50,000 excluding configs_i), the energy error of the FP32 path, the
-end-to-end rate through the public API with host buffers, the roofline of the
-enumeration kernel, and the CPU oracle's rate on the host cores.
+one energy-gradient evaluation.  The metric is term applications per second
+counted as the reference counts them: T * (N_i + N_j) per step (the
+reference's thread grid is T * N_i for a forward application, T * N_j for
+the same kernel run on the daggered table from configs_j).  The walks here
+visit fewer pairs (both directions walk the 20,000 configs_i rows);
+``walked_pairs_per_s`` reports that count, 2 * T * N_i per step.  The same
+line reports the FP64 path, the reference's own CUDA apply_within run from
+its cubin (``ref_cuda_fp64``), find_relative (top 50,000 excluding
+configs_i), the energy error of the FP32 path, the end-to-end rate through
+the public API with host buffers, the rooflines of the term walk, and the
+CPU oracle's rate on the host cores.
 
-``--impl reference`` times the CPU restatement of the reference engine
-(oracle/, the reference's own CPU code cannot be built on the GPU host) on a
-bounded sample of the same workload with every host core.
+``--impl reference`` times the reference's CPU algorithm (the oracle port in
+oracle/, bit-identical to the reference's _hamiltonian_cpu.cpp and within 16 %
+of its speed on one core where both run) on a bounded sample of every step:
+the forward over a slice of configs_i and the adjoint, as the reference
+would compute it (its apply_within on the daggered table from configs_j
+onto configs_i), over a slice of configs_j, on every host core.
+
+``--workload c1|c3|c4|c5|lanczos|pt2`` runs the other shapes (one JSON line
+each, clocked, L2 flushed before every timed step, with a roofline).
 """
 
 from __future__ import annotations
@@ -96,46 +107,112 @@ def make_workload(name: str):
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle timing (reference arm and cpu_baseline)
+# CPU timing of the reference's algorithm (the oracle port): reference arm and
+# cpu_baseline
 # ---------------------------------------------------------------------------
 
+_CPU = {}
 
-def _oracle_worker(args):
-    site, kind, coef, rows, psi, configs_j, budget_s, chunk = args
+
+def _cpu_init(site, kind, coef, ci, psi, cj, g):
+    """Worker set-up: both directions' tables, rows and amplitudes, targets sorted once.
+
+    The reference sorts configs_j once per apply_within call (thrust /
+    std::sort) and then walks T * N_i pairs; a sample that calls the oracle
+    once per slice would re-sort per slice, so the sort is done here, once,
+    and the timed jobs run the loop alone.
+    """
     sys.path.insert(0, REPO)
-    import oracle
-
-    done = 0
-    start = time.perf_counter()
-    while done < rows.shape[0] and time.perf_counter() - start < budget_s:
-        hi = min(done + chunk, rows.shape[0])
-        oracle.apply_within(site, kind, coef, rows[done:hi], psi[done:hi], configs_j)
-        done = hi
-    return done, time.perf_counter() - start
-
-
-def oracle_rate(wl, budget_s: float, cores: int | None = None) -> dict:
-    """Term applications per second of the CPU oracle's apply_within, every host core on a row slice."""
     import numpy as np
 
     import oracle
+    from oracle import ref_cuda
 
     oracle.build()
+    dsite, dkind, dcoef = ref_cuda.daggered(site, kind, coef)
+    c = lambda a, t: np.ascontiguousarray(a, dtype=t)
+    _CPU.update(
+        fwd=(c(site, np.int16), c(kind, np.uint8), c(coef, np.float64), c(ci, np.uint8),
+             c(np.asarray(psi).view(np.float64).reshape(-1, 2), np.float64), c(cj, np.uint8)),
+        adj=(c(dsite, np.int16), c(dkind, np.uint8), c(dcoef, np.float64), c(cj, np.uint8),
+             c(np.asarray(g).view(np.float64).reshape(-1, 2), np.float64), c(ci, np.uint8)))
+    _CPU["idx_fwd"] = oracle.sort_rows(_CPU["fwd"][5])
+    _CPU["idx_adj"] = oracle.sort_rows(_CPU["adj"][5])
+    _CPU["acc_fwd"] = np.zeros((cj.shape[0], 2))
+    _CPU["acc_adj"] = np.zeros((ci.shape[0], 2))
+
+
+def _cpu_job(job):
+    """One slice of one direction: (direction, first row, end row) -> (pairs walked, seconds)."""
+    import oracle
+
+    direction, a, b = job
+    site, kind, coef, src, psi, dst = _CPU[direction]
+    t0 = time.perf_counter()
+    oracle.apply_within_sorted(site, kind, coef, src, psi, dst, _CPU["idx_" + direction], _CPU["acc_" + direction],
+                               (a, b))
+    return site.shape[0] * (b - a), time.perf_counter() - t0
+
+
+class CpuReference:
+    """The reference's CPU apply_within (oracle port) on `cores` processes, forward and adjoint slices per step."""
+
+    def __init__(self, wl, cores: int):
+        import concurrent.futures
+
+        import numpy as np
+
+        rng = np.random.default_rng(7)
+        g = rng.standard_normal(wl["configs_j"].shape[0]) + 1j * rng.standard_normal(wl["configs_j"].shape[0])
+        self.cores = cores
+        self.n_i, self.n_j = wl["configs_i"].shape[0], wl["configs_j"].shape[0]
+        self.T = wl["n_terms"]
+        self.pool = concurrent.futures.ProcessPoolExecutor(
+            cores, mp_context=mp.get_context("spawn"), initializer=_cpu_init,
+            initargs=(wl["site"], wl["kind"], wl["coef"], wl["configs_i"], wl["psi"], wl["configs_j"], g))
+        self.cursor = 0
+
+    def step(self, fraction: float) -> tuple[float, float]:
+        """One sampled step: `fraction` of the forward rows and of the adjoint rows; returns (pairs, wall seconds)."""
+        n_f = max(1, int(round(fraction * self.n_i)))
+        n_a = max(1, int(round(fraction * self.n_j)))
+        jobs = []
+        for direction, n, total in (("fwd", n_f, self.n_i), ("adj", n_a, self.n_j)):
+            a0 = (self.cursor * n) % max(total - n + 1, 1)
+            per = -(-n // self.cores)
+            for a in range(a0, a0 + n, per):
+                jobs.append((direction, a, min(a + per, a0 + n)))
+        self.cursor += 1
+        t0 = time.perf_counter()
+        done = list(self.pool.map(_cpu_job, jobs))
+        wall = time.perf_counter() - t0
+        return float(sum(d[0] for d in done)), wall
+
+    def close(self):
+        self.pool.shutdown()
+
+
+def cpu_reference_rate(wl, budget_s: float, cores: int | None = None, fraction: float | None = None) -> dict:
+    """Term applications per second of the reference's CPU algorithm over about budget_s of sampled steps."""
     cores = cores or os.cpu_count() or 1
-    rows = wl["configs_i"]
-    psi = wl["psi"]
-    slices = np.array_split(np.arange(rows.shape[0]), cores)
-    chunk = 16
-    jobs = [(wl["site"], wl["kind"], wl["coef"], rows[s], psi[s], wl["configs_j"], budget_s, chunk) for s in slices]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        results = pool.map(_oracle_worker, jobs)
-    done = sum(r[0] for r in results)
-    elapsed = max(r[1] for r in results)
-    rate = wl["n_terms"] * done / elapsed
-    return {"value": rate, "unit": "term-applications/s", "cores": cores, "kind": "port",
-            "sample": f"apply_within forward of {done} of {rows.shape[0]} configs_i rows against all "
-                      f"{wl['configs_j'].shape[0]} configs_j, {cores} processes, {elapsed:.1f} s"}
+    ref = CpuReference(wl, cores)
+    try:
+        frac = fraction or 0.02 * min(1.0, cores / 16)
+        ref.step(frac / 4)  # starts the workers (spawn + set-up) outside the timing
+        pairs = secs = 0.0
+        steps = 0
+        while secs < budget_s or steps == 0:
+            p, w = ref.step(frac)
+            pairs += p
+            secs += w
+            steps += 1
+    finally:
+        ref.close()
+    return {"value": pairs / secs, "unit": "term-applications/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of apply_within forward over {frac:.2%} of the {wl['configs_i'].shape[0]} "
+                      f"configs_i rows (targets: all {wl['configs_j'].shape[0]} configs_j) and adjoint over "
+                      f"{frac:.2%} of the configs_j rows (daggered table, targets: configs_i), {cores} processes, "
+                      f"{secs:.1f} s, targets sorted once per process"}
 
 
 # ---------------------------------------------------------------------------
@@ -229,33 +306,49 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_figure(workload: str, name: str):
-    """A per-launch figure of the term walk (`name: value`) from the committed ncu summary, or None."""
-    path = os.path.join(REPO, "profiles", f"term_walk_{workload}.md")
+# Sources whose change invalidates a committed ncu figure of the engine's kernels.
+KERNEL_SOURCES = ("qmb-public_gb300/csrc/device.cuh", "qmb-public_gb300/csrc/apply.cu",
+                  "qmb-public_gb300/csrc/keys.cu", "qmb-public_gb300/csrc/relative.cu",
+                  "qmb-public_gb300/csrc/format.h", "qmb-public_gb300/csrc/table.cpp")
+
+
+def kernel_sources_sha() -> str:
+    """First 16 hex digits of the SHA-256 over the kernel sources (see KERNEL_SOURCES)."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(REPO, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_figures(name: str) -> dict | None:
+    """Per-launch ncu figures committed as profiles/<name>.json, or None when absent or
+    taken on kernel sources other than the current ones (a stale figure is never used)."""
+    path = os.path.join(REPO, "profiles", f"{name}.json")
     try:
-        text = open(path).read()
-    except OSError:
+        with open(path) as f:
+            figs = json.load(f)
+    except (OSError, ValueError):
         return None
-    m = re.search(name + r":\s*([0-9.eE+]+)", text)
-    return float(m.group(1)) if m else None
+    if figs.get("kernel_sources_sha") != kernel_sources_sha():
+        return None
+    return figs
 
 
-def ncu_traffic(workload: str):
-    """DRAM bytes per enumeration launch from the committed ncu summary, or None."""
-    return ncu_figure(workload, "traffic_bytes_per_launch")
-
-
-def issue_roofline(workload: str, launch_ms: float, device, clocks: dict):
+def issue_roofline(figs: dict | None, launch_ms: float, device, clocks: dict):
     """The walk's binding resource: warp instructions issued per second against the SMs' issue slots.
 
     The walk is sparse integer work (bit tests, hashing, L2 lookups), so its
     HBM fraction is small by construction; this second roofline divides the
-    warp instructions of one launch (ncu, committed summary) by the live
-    launch time, against 4 issue slots per SM per clock at the sampled clock.
+    warp instructions of one launch (ncu, committed with the hash of the
+    kernel sources it was taken on) by the live launch time, against 4 issue
+    slots per SM per clock at the sampled clock.
     """
     import torch
 
-    inst = ncu_figure(workload, "warp_instructions_per_launch")
+    inst = (figs or {}).get("warp_instructions_per_launch")
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
     if inst is None or not mhz or launch_ms <= 0:
         return None
@@ -263,7 +356,86 @@ def issue_roofline(workload: str, launch_ms: float, device, clocks: dict):
     achieved = inst / (launch_ms * 1e-3)
     peak = sms * 4 * mhz * 1e6
     return {"achieved": achieved, "peak": peak, "unit": "warp-inst/s", "frac": achieved / peak,
-            "warp_instructions_per_launch": inst, "sms": sms, "sm_mhz": mhz}
+            "warp_instructions_per_launch": inst, "sms": sms, "sm_mhz": mhz,
+            "source": f"profiles/{figs.get('name', '')}.json (kernel sources {figs.get('kernel_sources_sha')})"}
+
+
+def hbm_roofline(alg_bytes: float, launch_ms: float, kernel: str, figs: dict | None = None, **extra) -> dict:
+    """The contract's roofline: algorithmic bytes per launch over the live launch time, against measured HBM."""
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9 if launch_ms > 0 else 0.0
+    line = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (figs or {}).get("traffic_bytes_per_launch"), "kernel": kernel,
+            "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
+            "peak_source": f"{peak_kind} hbm_gbs"}
+    line.update(extra)
+    return line
+
+
+def workload_config(args, wl) -> dict:
+    """The config both arms report (identical dicts, so the two lines compare)."""
+    return {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": wl["n_terms"],
+            "n_i": int(wl["configs_i"].shape[0]), "n_j": int(wl["configs_j"].shape[0]), "n_qubytes": wl["nq"],
+            "parallelism": f"replicas x{args.gpus}", "l2": "flushed (256 MB write) before every timed step"}
+
+
+def time_reference_cuda(wl, device, reps: int = 3) -> dict:
+    """The reference's own CUDA apply_within (its cubin, oracle/_ref) on the same workload, forward and adjoint.
+
+    The adjoint is what a user of the reference would run for H^dagger g: its
+    apply_within on the daggered table from configs_j onto configs_i.
+    """
+    import numpy as np
+    import torch
+
+    from oracle import ref_cuda
+
+    nq = wl["nq"]
+    if not ref_cuda.available(nq, 1):
+        return {"unavailable": f"no reference cubin for n_qubytes {nq} in oracle/_ref (built from the reference's "
+                               "sources by oracle/ref_build.py where they are present)"}
+    ref = ref_cuda.ReferenceCuda(nq, 1, device)
+    fwd = ref.table(wl["site"], wl["kind"], wl["coef"])
+    adj = ref.table(*ref_cuda.daggered(wl["site"], wl["kind"], wl["coef"]))
+    ci = torch.from_numpy(wl["configs_i"]).to(device)
+    cj = torch.from_numpy(wl["configs_j"]).to(device)
+    psi = torch.from_numpy(wl["psi"]).to(device)
+    stream = torch.cuda.current_stream(device)
+
+    def timed(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            out = fn()
+            b.record(stream)
+            ts.append((a, b))
+        torch.cuda.synchronize(device)
+        return out, sum(a.elapsed_time(b) for a, b in ts) / reps
+
+    y, ms_fwd = timed(lambda: ref.apply_within(fwd, ci, psi, cj))
+    x, ms_adj = timed(lambda: ref.apply_within(adj, cj, y, ci))
+    # kernel alone, targets presorted
+    perm = ref.sort_rows(cj)
+    sorted_j = cj[perm].contiguous()
+    acc = torch.zeros((cj.shape[0], 2), dtype=torch.float64, device=device)
+    psi_f = torch.view_as_real(psi).contiguous()
+
+    def kernel_only():
+        acc.zero_()
+        ref.launch(fwd, ci, psi_f, sorted_j, acc, stream.cuda_stream)
+
+    _, ms_kernel = timed(kernel_only)
+    T = wl["n_terms"]
+    units = T * (ci.shape[0] + cj.shape[0])
+    return {"fwd_ms": ms_fwd, "adj_ms": ms_adj, "step_ms": ms_fwd + ms_adj, "fwd_kernel_ms": ms_kernel,
+            "value": units / ((ms_fwd + ms_adj) * 1e-3), "unit": "term-applications/s",
+            "y": y, "x": x,
+            "what": "qmb/_hamiltonian_cuda.cu apply_within_kernel_interface from the reference's own sources "
+                    "(oracle/ref_build.py), host side replayed with torch (targets sorted by a stable byte-wise "
+                    "LSD sort in place of thrust::sort_by_key); adjoint = the same kernel on the daggered table "
+                    "from configs_j onto configs_i"}
 
 
 def run_ours(args, wl, rank: int, world: int) -> dict | None:
@@ -333,16 +505,12 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
 
     ms64 = timed(step64, args.steps)
 
-    # find_relative (top K excluding configs_i)
+    # find_relative (top K excluding configs_i); it synchronises, so it is timed on its own
     K = wl["spec"]["count_selected"]
     ham.find_relative(ci, psi64, K)
-    torch.cuda.synchronize(device)
-    t0 = time.perf_counter()
     reps = max(1, min(args.steps, 5))
-    for _ in range(reps):
-        rel = ham.find_relative(ci, psi64, K)
-    torch.cuda.synchronize(device)
-    ms_rel = (time.perf_counter() - t0) * 1e3 / reps
+    ms_rel = timed(lambda: ham.find_relative(ci, psi64, K), reps) / reps
+    rel = ham.find_relative(ci, psi64, K)
 
     # energy error of the FP32 path on the configs_i block
     e64 = float(qmb.variational_energy(ham, ci, psi32.to(torch.complex128)))
@@ -371,29 +539,47 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     d2h = y_h.numel() * 8 + x_h.numel() * 8
     ms32, ms64, ms_e2e = max_over_ranks([ms32, ms64, ms_e2e], device)
 
-    # per-kernel-group device time, in a separate profiled pass of the same step
+    # per-kernel-group device time, in separate profiled passes of the same step and of find_relative
     native.profile_enable(True)
     timed(step32, args.steps)
     torch.cuda.synchronize(device)
     prof = native.profile_read()
+    native.profile_enable(True)
+    timed(lambda: ham.find_relative(ci, psi64, K), reps)
+    prof_rel = native.profile_read()
+    stats_rel = native.find_relative_stats()
     native.profile_enable(False)
     n_enum, ms_enum = prof["groups"]["enumerate"]
 
     if rank != 0:
         return None
-    cpu = oracle_rate(wl, budget_s=args.cpu_seconds) if world == 1 else None
+    cpu = cpu_reference_rate(wl, budget_s=args.cpu_seconds) if world == 1 else None
+    try:
+        ref_cuda = time_reference_cuda(wl, device)
+        if "y" in ref_cuda:
+            y_ref, x_ref = ref_cuda.pop("y"), ref_cuda.pop("x")
+            y_our = ham.apply_within(ci, psi64, cj)
+            x_our = ham.apply_within_adjoint(ci, y_ref, cj)
+            ref_cuda["max_abs_diff_vs_engine_fp64"] = max((y_our - y_ref).abs().max().item(),
+                                                         (x_our - x_ref).abs().max().item())
+            ref_cuda["engine_fp64_speedup"] = ref_cuda["step_ms"] / (ms64 / args.steps)
+            ref_cuda["engine_fp32c_speedup"] = ref_cuda["step_ms"] / (ms32 / args.steps)
+    except (RuntimeError, OSError) as exc:  # a missing driver entry point or cubin load failure
+        ref_cuda = {"unavailable": f"{type(exc).__name__}: {exc}"}
 
-    # roofline of the enumeration kernel: algorithmic bytes per launch
+    # roofline of the term walk: algorithmic bytes per launch
     # forward: targets N_j (key + FP64 result), sources N_i (key + FP32 amplitude), terms T (28 B)
     # adjoint: the same with the two sets swapped
     alg_fwd = n_j * (nq + 16) + n_i * (nq + 8) + T * 28
     alg_adj = n_i * (nq + 16) + n_j * (nq + 8) + T * 28
     alg = (alg_fwd + alg_adj) / 2
     per_launch_ms = ms_enum / max(n_enum, 1)
-    peak, peak_kind = measured_peaks()
-    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    figs = ncu_figures(f"term_walk_{args.workload}")
     ms_step32 = ms32 / args.steps
     value = replica_value(units, ms_step32, world)
+    # the radix sorts of find_relative: passes x 2 x records x record bytes over their device time
+    n_sort, ms_sort = prof_rel["groups"]["sort"]
+    sort_bytes = reps * stats_rel["sort_bytes"]
     line = {
         "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
         "value": value,
@@ -407,25 +593,28 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": T, "n_i": n_i, "n_j": n_j,
-                   "n_qubytes": nq, "parallelism": f"replicas x{world}",
-                   "l2": "flushed (256 MB write) before every timed step"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ncu_traffic(args.workload), "kernel": "term walk (grouped_kernel)",
-                     "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_ms,
-                     "peak_source": f"{peak_kind} hbm_gbs"},
-        "issue_roofline": issue_roofline(args.workload, per_launch_ms, device, clocks.summary()),
+        "config": workload_config(args, wl),
+        "roofline": hbm_roofline(alg, per_launch_ms, "term walk (grouped_kernel)", figs),
+        "issue_roofline": issue_roofline(figs, per_launch_ms, device, clocks.summary()),
         "cpu_baseline": cpu,
         "e2e": {"value": world * units / (ms_e2e / args.steps * 1e-3), "unit": "term-applications/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "walked_pairs_per_s": {"value": world * 2 * T * n_i / (ms_step32 * 1e-3),
+                               "what": "(term, row) pairs the walks visit: both directions walk configs_i's "
+                                       f"{n_i} rows, 2 * T * N_i = {2 * T * n_i:.3e} per step"},
         "fp64": {"value": world * units / (ms64 / args.steps * 1e-3), "ms_per_step": ms64 / args.steps},
         "speedup_fp32c_vs_fp64": ms64 / ms32,
-        "find_relative": {"ms": ms_rel, "count_selected": K, "rows_out": int(rel.shape[0])},
+        "ref_cuda_fp64": ref_cuda,
+        "find_relative": {"ms": ms_rel, "count_selected": K, "rows_out": int(rel.shape[0]),
+                          "kernel_groups_ms": {g: prof_rel["groups"][g][1] / reps for g in prof_rel["groups"]},
+                          "stats": stats_rel,
+                          "sort_roofline": hbm_roofline(sort_bytes, ms_sort, "radix sorts (radix_hist/scatter + scans)",
+                                                        None, launches=n_sort) if ms_sort > 0 else None},
         "energy": {"fp64": e64, "fp32c": e32, "abs_error_ha": abs(e32 - e64)},
         "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]},
-        "clock_window": "nvidia-smi every 50 ms across the FP32c, FP64 and end-to-end timed loops",
+        "clock_window": "nvidia-smi every 50 ms across the FP32c, FP64, find_relative and end-to-end timed loops",
     }
     return line
 
@@ -462,6 +651,7 @@ class _Mlp:
 
 
 def _timed_loop(fn, steps, device, flush=None):
+    """Mean milliseconds of fn over `steps` runs: CUDA events on the current stream, L2 flushed before each run."""
     import torch
 
     stream = torch.cuda.current_stream(device)
@@ -479,134 +669,203 @@ def _timed_loop(fn, steps, device, flush=None):
     return sum(a.elapsed_time(b) for a, b in pairs) / steps
 
 
+def _profiled(native, fn, device):
+    """Per-group (launches, ms) of one run of fn."""
+    import torch
+
+    native.profile_enable(True)
+    fn()
+    torch.cuda.synchronize(device)
+    prof = native.profile_read()
+    native.profile_enable(False)
+    return prof
+
+
 def run_extra(args, wl) -> dict:
-    """The other benchmark shapes: c3 (energy + gradient through an MLP), c4 (Hubbard 1M), c5 (find_relative 1M),
-    and the engine's callers: lanczos (20 iterations on the c3 basis) and pt2 (one PT2 step on the c5 shape)."""
+    """The other benchmark shapes: c1 (all 400 determinants of 12 spin orbitals), c3 (energy + gradient through
+    an MLP), c4 (Hubbard 1M), c5 (find_relative 1M), and the engine's callers: lanczos (20 iterations on the c3
+    basis) and pt2 (one PT2 step on the c5 shape).  Every line is clocked (nvidia-smi across the timed loops),
+    flushes L2 before every timed step and carries the roofline of its dominant kernel group."""
     import torch
 
     qmb = importlib.import_module("qmb-public_gb300")
     native = importlib.import_module("qmb-public_gb300._native")
     device = torch.device("cuda", 0)
-    kind = "fermi"
     ham = qmb.Hamiltonian((torch.from_numpy(wl["site"]), torch.from_numpy(wl["kind"]), torch.from_numpy(wl["coef"])),
-                          kind=kind)
+                          kind="fermi")
     ci = torch.from_numpy(wl["configs_i"]).to(device)
+    cj = torch.from_numpy(wl["configs_j"]).to(device)
     T, nq, n = wl["n_terms"], wl["nq"], ci.shape[0]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
-    line = {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": T, "n_rows": n, "n_qubytes": nq}
+    line = {"config": workload_config(args, wl), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "data": "synthetic", "vs_baseline": None, "scaling": "weak"}
+    clocks = ClockSampler(device.index)
+    walk_alg = lambda n_walk, n_look, amp: n_walk * (nq + 16) + n_look * (nq + amp) + T * 28
+
+    def walk_roofline(prof, n_walk, n_look, amp, kernel):
+        cnt, ms = prof["groups"]["enumerate"]
+        return hbm_roofline(walk_alg(n_walk, n_look, amp), ms / max(cnt, 1), kernel,
+                            ncu_figures(f"term_walk_{args.workload}"), launches=cnt)
+
     if args.workload == "c3":
         mlp = _Mlp(8 * nq, device, seed=wl["spec"]["seed"])
 
-        def step(dtype):
+        def step(dtype, shortcut=True):
             for p in mlp.net.parameters():
                 p.grad = None
             psi = mlp(ci)
-            e = qmb.variational_energy(ham, ci, psi if dtype == torch.complex64 else psi.to(torch.complex128))
+            e = qmb.variational_energy(ham, ci, psi if dtype == torch.complex64 else psi.to(torch.complex128),
+                                       hermitian_shortcut=shortcut)
             e.backward()
             return e
 
         for _ in range(args.warmup):
             step(torch.complex64)
             step(torch.complex128)
-        native.profile_enable(True)
-        ms32 = _timed_loop(lambda: step(torch.complex64), args.steps, device, flush)
-        prof = native.profile_read()
-        native.profile_enable(False)
-        ms64 = _timed_loop(lambda: step(torch.complex128), args.steps, device, flush)
+            step(torch.complex64, False)
+        with clocks:
+            ms32 = _timed_loop(lambda: step(torch.complex64), args.steps, device, flush)
+            ms64 = _timed_loop(lambda: step(torch.complex128), args.steps, device, flush)
+            ms32_adj = _timed_loop(lambda: step(torch.complex64, False), args.steps, device, flush)
+            ms64_adj = _timed_loop(lambda: step(torch.complex128, False), args.steps, device, flush)
+        prof = _profiled(native, lambda: step(torch.complex64), device)
+        prof_adj = _profiled(native, lambda: step(torch.complex64, False), device)
         e32 = float(step(torch.complex64).detach())
         e64 = float(step(torch.complex128).detach())
         line.update({"metric": "energy forward + backward step (FP32-compensated)", "value": ms32, "unit": "ms",
-                     "higher_is_better": False, "fp64_ms": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "ms_per_step": ms32, "higher_is_better": False, "dtype": "f32", "fp64_ms": ms64,
+                     "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "through_adjoint_kernel": {"fp32c_ms": ms32_adj, "fp64_ms": ms64_adj,
+                                                "speedup_fp32c_vs_fp64": ms64_adj / ms32_adj,
+                                                "walks_per_step": prof_adj["groups"]["enumerate"][0],
+                                                "kernel_groups_ms": {g: v[1] for g, v in prof_adj["groups"].items()}},
                      "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),
                      "hermitian": ham._table(device, nq).hermitian,
-                     "walks_per_step": prof["groups"]["enumerate"][0] / args.steps,
-                     "apply_term_applications_per_s": prof["groups"]["enumerate"][0] * T * n / (prof["groups"]["enumerate"][1] * 1e-3),
-                     "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]}})
-    elif args.workload == "c4":
+                     "walks_per_step": prof["groups"]["enumerate"][0],
+                     "roofline": walk_roofline(prof, n, n, 8, "term walk (pivot_kernel)"),
+                     "kernel_groups_ms_per_step": {g: v[1] for g, v in prof["groups"].items()}})
+    elif args.workload in ("c1", "c4"):
         psi32 = torch.from_numpy(wl["psi"]).to(torch.complex64).to(device)
         psi64 = psi32.to(torch.complex128)
 
         def step32():
-            y = ham.apply_within(ci, psi32, ci)
-            return ham.apply_within_adjoint(ci, y, ci)
+            y = ham.apply_within(ci, psi32, cj)
+            return ham.apply_within_adjoint(ci, y, cj)
 
         def step64():
-            y = ham.apply_within(ci, psi64, ci)
-            return ham.apply_within_adjoint(ci, y, ci)
+            y = ham.apply_within(ci, psi64, cj)
+            return ham.apply_within_adjoint(ci, y, cj)
 
         for _ in range(args.warmup):
             step32()
             step64()
-        ms32 = _timed_loop(step32, args.steps, device, flush)
-        ms64 = _timed_loop(step64, args.steps, device, flush)
+        with clocks:
+            ms32 = _timed_loop(step32, args.steps, device, flush)
+            ms64 = _timed_loop(step64, args.steps, device, flush)
+        prof = _profiled(native, step32, device)
         e32 = float(qmb.variational_energy(ham, ci, psi32))
         e64 = float(qmb.variational_energy(ham, ci, psi64))
+        units = T * (ci.shape[0] + cj.shape[0])
         line.update({"metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
-                     "value": 2 * T * n / (ms32 * 1e-3), "unit": "term-applications/s", "higher_is_better": True,
-                     "ms_per_step": ms32, "fp64_ms_per_step": ms64, "speedup_fp32c_vs_fp64": ms64 / ms32,
-                     "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64)})
+                     "value": units / (ms32 * 1e-3), "unit": "term-applications/s", "higher_is_better": True,
+                     "dtype": "f32", "ms_per_step": ms32, "fp64_ms_per_step": ms64,
+                     "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),
+                     "roofline": walk_roofline(prof, n, cj.shape[0], 8, "term walk"),
+                     "kernel_groups_ms_per_step": {g: v[1] for g, v in prof["groups"].items()}})
     elif args.workload == "lanczos":
         n_steps = wl["spec"]["lanczos_steps"]
         gen = torch.Generator(device=device).manual_seed(wl["spec"]["seed"])
         start = torch.randn([n], dtype=torch.complex128, device=device, generator=gen)
         for _ in range(args.warmup):
             qmb.lanczos_energy(ham, ci, 2, start=start)
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            energy, _vec = qmb.lanczos_energy(ham, ci, n_steps, start=start)
-        torch.cuda.synchronize(device)
-        ms = (time.perf_counter() - t0) * 1e3 / args.steps
-        native.profile_enable(True)
-        qmb.lanczos_energy(ham, ci, n_steps, start=start)
-        torch.cuda.synchronize(device)
-        prof = native.profile_read()
-        native.profile_enable(False)
-        n_apply = n_steps + 2
+        result = {}
+
+        def run():
+            result["e"] = qmb.lanczos_energy(ham, ci, n_steps, start=start)[0]
+
+        with clocks:
+            ms = _timed_loop(run, args.steps, device, flush)
+        prof = _profiled(native, run, device)
+        n_apply = prof["groups"]["enumerate"][0]
         line.update({"metric": "Lanczos wall time (20 iterations, FP64, Ritz value on the host)", "value": ms,
-                     "unit": "ms", "higher_is_better": False, "ms_per_iteration": ms / n_apply,
-                     "energy": energy, "apply_within_calls": n_apply,
-                     "term_applications_per_s": n_apply * T * n / (ms * 1e-3),
-                     "kernel_groups_ms_per_run": {g: prof["groups"][g][1] for g in prof["groups"]}})
+                     "unit": "ms", "ms_per_step": ms, "higher_is_better": False, "dtype": "f64",
+                     "ms_per_iteration": ms / (n_steps + 2), "energy": result["e"], "walks": n_apply,
+                     "term_applications_per_s": (n_steps + 2) * T * n / (ms * 1e-3),
+                     "roofline": walk_roofline(prof, n, n, 16, "term walk"),
+                     "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
     elif args.workload == "pt2":
         psi = torch.from_numpy(wl["psi"]).to(device)
         K = wl["spec"]["count_selected"]
         for _ in range(args.warmup):
             qmb.pt2_energy(ham, ci, psi, K)
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e0, e2 = qmb.pt2_energy(ham, ci, psi, K)
-        torch.cuda.synchronize(device)
-        ms = (time.perf_counter() - t0) * 1e3 / args.steps
-        native.profile_enable(True)
-        qmb.pt2_energy(ham, ci, psi, K)
-        torch.cuda.synchronize(device)
-        prof = native.profile_read()
-        native.profile_enable(False)
-        line.update({"metric": "PT2 step wall time (E0, find_relative, H psi on the selected rows, denominators)",
-                     "value": ms, "unit": "ms", "higher_is_better": False, "count_selected": K, "e0": e0, "e2": e2,
-                     "kernel_groups_ms_per_run": {g: prof["groups"][g][1] for g in prof["groups"]}})
-    else:
+        result = {}
+
+        def run():
+            result["e"] = qmb.pt2_energy(ham, ci, psi, K)
+
+        with clocks:
+            ms = _timed_loop(run, args.steps, device, flush)
+        prof = _profiled(native, run, device)
+        line.update({"metric": "PT2 step wall time (E0, selection of the connected space, H psi on it, "
+                               "denominators, Epstein-Nesbet sum)", "value": ms, "unit": "ms", "ms_per_step": ms,
+                     "higher_is_better": False, "dtype": "f64", "count_selected": K, "e0": result["e"][0],
+                     "e2": result["e"][1],
+                     "roofline": walk_roofline(prof, n, n, 16, "term walk"),
+                     "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
+    else:  # c5: find_relative
         psi = torch.from_numpy(wl["psi"]).to(device)
         K = wl["spec"]["count_selected"]
         rel = ham.find_relative(ci, psi, K)
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(args.warmup):
             rel = ham.find_relative(ci, psi, K)
-        torch.cuda.synchronize(device)
-        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        with clocks:
+            ms = _timed_loop(lambda: ham.find_relative(ci, psi, K), args.steps, device, flush)
+        prof = _profiled(native, lambda: ham.find_relative(ci, psi, K), device)
+        stats = native.find_relative_stats()
+        n_sort, ms_sort = prof["groups"]["sort"]
         line.update({"metric": "find_relative wall time (top K of all connected records)", "value": ms, "unit": "ms",
-                     "higher_is_better": False, "count_selected": K, "rows_out": int(rel.shape[0]),
-                     "term_applications_per_s": T * n / (ms * 1e-3)})
-    line.update({"steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic"})
+                     "ms_per_step": ms, "higher_is_better": False, "dtype": "f64", "count_selected": K,
+                     "rows_out": int(rel.shape[0]), "term_applications_per_s": T * n / (ms * 1e-3),
+                     "stats": stats,
+                     "roofline": walk_roofline(prof, n, ci.shape[0], 16, "term walk (pivot_kernel)"),
+                     "sort_roofline": hbm_roofline(stats["sort_bytes"], ms_sort, "radix sorts", None,
+                                                   launches=n_sort) if ms_sort > 0 else None,
+                     "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
+    line["clocks"] = clocks.summary()
     return line
 
 
 def run_reference(args, wl) -> dict:
-    cpu = oracle_rate(wl, budget_s=args.cpu_seconds)
-    value = cpu["value"]
+    """The reference arm: the reference's CPU algorithm on every host core, K sampled steps after W warm-up ones.
+
+    Each step walks the same fraction of the forward rows (configs_i against
+    configs_j) and of the adjoint rows (configs_j against configs_i with the
+    daggered table, the reference's way to apply H^dagger), split across the
+    host cores; the value is the pairs walked over the wall time.  A 1-core
+    figure rides along (the reference's CPU loops are serial).
+    """
+    cores = os.cpu_count() or 1
+    frac = args.ref_fraction
+    ref = CpuReference(wl, cores)
+    try:
+        for _ in range(max(args.warmup, 1)):
+            ref.step(frac)
+        pairs = secs = 0.0
+        times = []
+        for _ in range(args.steps):
+            p, w = ref.step(frac)
+            pairs += p
+            secs += w
+            times.append(w)
+    finally:
+        ref.close()
+    value = pairs / secs
+    one = cpu_reference_rate(wl, budget_s=2.0, cores=1, fraction=frac / 16)
+    n_i, n_j = wl["configs_i"].shape[0], wl["configs_j"].shape[0]
+    sample = (f"each step: apply_within forward over {frac:.2%} of the {n_i} configs_i rows (targets: all {n_j} "
+              f"configs_j) and adjoint over {frac:.2%} of the {n_j} configs_j rows (daggered table, targets: "
+              f"configs_i), split over {cores} processes; targets sorted once per process")
     return {
         "impl": "reference",
         "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
@@ -615,17 +874,19 @@ def run_reference(args, wl) -> dict:
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": wl["n_terms"] * (wl["configs_i"].shape[0] + wl["configs_j"].shape[0]) / value * 1e3,
+        "ms_per_step": secs * 1e3 / max(args.steps, 1),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {wl['spec']['description']}", "n_terms": wl["n_terms"],
-                   "n_i": int(wl["configs_i"].shape[0]), "n_j": int(wl["configs_j"].shape[0]),
-                   "n_qubytes": wl["nq"]},
-        "cpu_baseline": cpu,
+        "config": workload_config(args, wl),
+        "cpu_baseline": {"value": value, "unit": "term-applications/s", "cores": cores, "kind": "port",
+                         "sample": sample, "one_core": one,
+                         "step_ms_min_max": [min(times) * 1e3, max(times) * 1e3]},
         "e2e": {"value": value, "unit": "term-applications/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "what": "the oracle port of qmb/_hamiltonian_cpu.cpp (bit-identical results; within 16 % of the "
+                "reference's own build on one core where both run), on a sample of every step",
     }
 
 
@@ -636,7 +897,9 @@ def main():
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
-    parser.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU oracle sample")
+    parser.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the cpu_baseline sample")
+    parser.add_argument("--ref-fraction", type=float, default=0.02,
+                        help="fraction of each direction's rows a reference-arm step walks")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -650,7 +913,7 @@ def main():
 
     import torch
 
-    if args.workload in ("c3", "c4", "c5", "lanczos", "pt2"):
+    if args.workload in ("c1", "c3", "c4", "c5", "lanczos", "pt2"):
         if rank == 0:
             print(json.dumps(run_extra(args, make_workload(args.workload))), flush=True)
         return

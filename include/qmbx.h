@@ -184,6 +184,13 @@ int qmbx_find_relative(const void* table_host, const void* table_dev, const uint
                        uint8_t* out, int64_t* n_out, void* workspace, uint64_t workspace_bytes,
                        uint64_t* workspace_needed, qmbx_stream_t stream);
 
+/* Figures of the calling thread's last qmbx_find_relative call, for tracing
+ * and rooflines (no counterpart in the reference): [0] records emitted by the
+ * selection pass, [1] term walks run, [2] radix passes over records and
+ * selected rows, [3] bytes those passes move (passes x 2 x items x item
+ * bytes), [4] records selected before de-duplication, [5] rows returned. */
+int qmbx_find_relative_stats(int64_t stats[6]);
+
 /* ---------------------------------------------------------------------------
  * single_relative: for every row, one image outside the row set drawn with
  * probability proportional to |coef_t| (Efraimidis-Spirakis keys from a
@@ -201,14 +208,16 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
 /* ---------------------------------------------------------------------------
  * Tracing (no counterpart in the reference, which has none).
  * Every kernel launch of this library increments a process-wide counter.
- * qmbx_profile_enable(1) additionally brackets the launches of five groups
- * (0 term walk, 1 key packing/sorting/hashing, 2 selection, 3 other,
- * 4 the separate passes over diagonal terms) with
- * CUDA events on the launching stream and resets the totals;
- * qmbx_profile_read waits for the recorded events and returns the launch
- * counter and, per group, the number of timed launches and their total
- * milliseconds (arrays of 5).
+ * qmbx_profile_enable(1) additionally brackets the launches of six groups
+ * (0 term walk, 1 key packing/hashing, 2 selection, 3 other, 4 the separate
+ * passes over diagonal terms, 5 radix sorts) with CUDA events on the
+ * launching stream and resets the totals; qmbx_profile_read waits for the
+ * recorded events and returns the launch counter and, per group, the number
+ * of timed launches and their total milliseconds (arrays of
+ * QMBX_PROFILE_GROUPS).
  * ------------------------------------------------------------------------- */
+
+#define QMBX_PROFILE_GROUPS 6
 
 int qmbx_profile_enable(int32_t on);
 

@@ -53,6 +53,12 @@ def _load() -> ctypes.CDLL:
         lib.oracle_term_uniform.restype = ctypes.c_double
         lib.oracle_single_relative.argtypes = [i32, i32, i64, p, p, p, i64, p, ctypes.c_uint64, p, p, p]
         lib.oracle_dense_matrix.argtypes = [i32, i32, i64, p, p, p, i64, p, p]
+        lib.oracle_apply_within_adjoint.argtypes = [i32, i32, i64, p, p, p, i64, i64, p, i64, p, p, p]
+        lib.oracle_relative_top_records.argtypes = [i32, i32, i64, p, p, p, i64, i64, i64, p, p, i64, i64, p, p, p, p]
+        lib.oracle_relative_top_records.restype = i64
+        lib.oracle_dense_columns.argtypes = [i32, i32, i64, p, p, p, i64, p, i64, i64, p]
+        lib.oracle_sort_rows.argtypes = [p, i64, i32, p]
+        lib.oracle_apply_within_sorted.argtypes = [i32, i32, i64, p, p, p, i64, i64, p, p, i64, p, p, p]
         _lib = lib
     return _lib
 
@@ -99,6 +105,78 @@ def apply_within(site, kind, coef, configs_i, psi_i, configs_j, particle_cut: in
     lib.oracle_apply_within(nq, particle_cut, site.shape[0], _ptr(site), _ptr(kind), _ptr(coef), ci.shape[0], _ptr(ci),
                             _ptr(pi), cj.shape[0], _ptr(cj), _ptr(out))
     return out.view(np.complex128).reshape(-1)
+
+
+def sort_rows(rows) -> np.ndarray:
+    """Stable lexicographic order of uint8 rows (int64 indices)."""
+    r = _c(rows, np.uint8)
+    idx = np.zeros(r.shape[0], dtype=np.int64)
+    _load().oracle_sort_rows(_ptr(r), r.shape[0], r.shape[1], _ptr(idx))
+    return idx
+
+
+def apply_within_sorted(site, kind, coef, configs_i, psi_f64, configs_j, idx, acc, rows, particle_cut: int = 1) -> None:
+    """apply_within's loop over source rows [begin, end) into acc (float64 [n_j, 2], by sorted position of configs_j).
+
+    Inputs must already be contiguous in the oracle's dtypes (psi_f64 float64
+    [n_i, 2]); nothing is copied, so timing loops measure the loop alone.
+    """
+    begin, end = rows
+    _load().oracle_apply_within_sorted(configs_i.shape[1], particle_cut, site.shape[0], _ptr(site), _ptr(kind),
+                                       _ptr(coef), begin, end, _ptr(configs_i), _ptr(psi_f64), configs_j.shape[0],
+                                       _ptr(configs_j), _ptr(idx), _ptr(acc))
+
+
+def apply_within_adjoint(site, kind, coef, configs_i, configs_j, g_j, particle_cut: int = 1, rows=None) -> np.ndarray:
+    """out_i = H^dagger g_j restricted to configs_i (rows = (begin, end) computes only those rows of configs_i)."""
+    lib = _load()
+    site, kind, coef = _table(site, kind, coef)
+    ci = _c(configs_i, np.uint8)
+    cj = _c(configs_j, np.uint8)
+    begin, end = (0, ci.shape[0]) if rows is None else rows
+    g = _psi(g_j)
+    out = np.zeros((max(end - begin, 0), 2), dtype=np.float64)
+    lib.oracle_apply_within_adjoint(ci.shape[1], particle_cut, site.shape[0], _ptr(site), _ptr(kind), _ptr(coef), begin,
+                                    end, _ptr(ci), cj.shape[0], _ptr(cj), _ptr(g), _ptr(out))
+    return out.view(np.complex128).reshape(-1)
+
+
+def relative_top_records(site, kind, coef, configs_i, psi_i, top: int, configs_exclude=None, particle_cut: int = 1,
+                         rows=None):
+    """The `top` highest-ranked find_relative records of source rows [begin, end) (all rows when rows is None).
+
+    Returns (weights, orders, rows): ranked order = weight descending, then
+    visiting order (term * n_i + row) descending; orders are those of the
+    whole configs_i, so results of separate row ranges merge exactly.
+    """
+    lib = _load()
+    site, kind, coef = _table(site, kind, coef)
+    ci = _c(configs_i, np.uint8)
+    ex = ci if configs_exclude is None else _c(configs_exclude, np.uint8)
+    nq = ci.shape[1]
+    pi = _psi(psi_i)
+    begin, end = (0, ci.shape[0]) if rows is None else rows
+    cap = max(int(top), 1)
+    w = np.zeros(cap, dtype=np.float64)
+    o = np.zeros(cap, dtype=np.uint64)
+    r = np.zeros((cap, nq), dtype=np.uint8)
+    n = lib.oracle_relative_top_records(nq, particle_cut, site.shape[0], _ptr(site), _ptr(kind), _ptr(coef), ci.shape[0],
+                                        begin, end, _ptr(ci), _ptr(pi), int(top), ex.shape[0], _ptr(ex), _ptr(w),
+                                        _ptr(o), _ptr(r))
+    return w[:n].copy(), o[:n].copy(), r[:n].copy()
+
+
+def dense_columns(site, kind, coef, configs, cols, particle_cut: int = 1) -> np.ndarray:
+    """Columns [begin, end) of the dense matrix <j|H|i> over configs: complex128 [n, end - begin]."""
+    lib = _load()
+    site, kind, coef = _table(site, kind, coef)
+    c = _c(configs, np.uint8)
+    n = c.shape[0]
+    begin, end = cols
+    mat = np.zeros((n, max(end - begin, 0), 2), dtype=np.float64)
+    lib.oracle_dense_columns(c.shape[1], particle_cut, site.shape[0], _ptr(site), _ptr(kind), _ptr(coef), n, _ptr(c),
+                             begin, end, _ptr(mat))
+    return mat.view(np.complex128).reshape(n, max(end - begin, 0))
 
 
 def diagonal_term(site, kind, coef, configs, particle_cut: int = 1) -> np.ndarray:

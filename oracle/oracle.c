@@ -126,22 +126,28 @@ static int64_t find_row(const uint8_t* rows, const int64_t* idx, int64_t n, cons
     return -1;
 }
 
+/* Stable lexicographic order of n rows into idx (the reference's sort of configs_j). */
+void oracle_sort_rows(const uint8_t* rows, int64_t n, int n_qubytes, int64_t* idx) {
+    int64_t* sorted = sorted_index(rows, n, n_qubytes);
+    memcpy(idx, sorted, (size_t)(n > 0 ? n : 0) * sizeof(int64_t));
+    free(sorted);
+}
+
 /*
- * apply_within (qmb/_hamiltonian_cpu.cpp:80-257): term-major double loop; for
- * every (term, source) whose image lies in configs_j, out[j] += sign*coef*psi.
- * The complex product is written exactly as in :127-128.  Where configs_j holds
- * duplicate rows, the whole amplitude goes to the first of them (lowest row
- * index); the reference gives it to one of them, chosen by its unstable sort.
+ * The loop of apply_within over sources [row_begin, row_end) with configs_j
+ * already sorted (idx from oracle_sort_rows): acc[pos] (complex, by sorted
+ * position) accumulates sign*coef*psi for every (term, source) whose image is
+ * the configs_j row at sorted position pos.  Split out so that timing runs can
+ * sort once and walk slices of the sources.
  */
-void oracle_apply_within(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site, const uint8_t* kind,
-                         const double* coef, int64_t n_i, const uint8_t* configs_i, const double* psi_i, int64_t n_j,
-                         const uint8_t* configs_j, double* psi_j) {
+void oracle_apply_within_sorted(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site,
+                                const uint8_t* kind, const double* coef, int64_t row_begin, int64_t row_end,
+                                const uint8_t* configs_i, const double* psi_i, int64_t n_j, const uint8_t* configs_j,
+                                const int64_t* idx, double* acc) {
     int nq = n_qubytes;
-    int64_t* idx = sorted_index(configs_j, n_j, nq);
-    double* acc = (double*)calloc((size_t)(n_j > 0 ? n_j : 1) * 2, sizeof(double));
     uint8_t* cur = (uint8_t*)malloc((size_t)nq);
     for (int64_t t = 0; t < n_terms; ++t) {
-        for (int64_t i = 0; i < n_i; ++i) {
+        for (int64_t i = row_begin; i < row_end; ++i) {
             memcpy(cur, configs_i + i * nq, (size_t)nq);
             int parity;
             if (!oracle_apply_term(nq, particle_cut, site + t * MAX_OPS, kind + t * MAX_OPS, cur, &parity)) {
@@ -158,13 +164,73 @@ void oracle_apply_within(int n_qubytes, int particle_cut, int64_t n_terms, const
             acc[2 * pos + 1] += sign * (c[0] * p[1] + c[1] * p[0]);
         }
     }
+    free(cur);
+}
+
+/*
+ * apply_within (qmb/_hamiltonian_cpu.cpp:80-257): term-major double loop; for
+ * every (term, source) whose image lies in configs_j, out[j] += sign*coef*psi.
+ * The complex product is written exactly as in :127-128.  Where configs_j holds
+ * duplicate rows, the whole amplitude goes to the first of them (lowest row
+ * index); the reference gives it to one of them, chosen by its unstable sort.
+ */
+void oracle_apply_within(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site, const uint8_t* kind,
+                         const double* coef, int64_t n_i, const uint8_t* configs_i, const double* psi_i, int64_t n_j,
+                         const uint8_t* configs_j, double* psi_j) {
+    int nq = n_qubytes;
+    int64_t* idx = sorted_index(configs_j, n_j, nq);
+    double* acc = (double*)calloc((size_t)(n_j > 0 ? n_j : 1) * 2, sizeof(double));
+    oracle_apply_within_sorted(nq, particle_cut, n_terms, site, kind, coef, 0, n_i, configs_i, psi_i, n_j, configs_j,
+                               idx, acc);
     memset(psi_j, 0, (size_t)n_j * 2 * sizeof(double));
     for (int64_t k = 0; k < n_j; ++k) {
         psi_j[2 * idx[k] + 0] = acc[2 * k + 0];
         psi_j[2 * idx[k] + 1] = acc[2 * k + 1];
     }
-    free(cur);
     free(acc);
+    free(idx);
+}
+
+/*
+ * The adjoint of apply_within (no counterpart in the reference, whose
+ * vmc.py:108-110 detaches H psi): out_i[i] = sum over terms t with
+ * t|i> = sign|j>, j in configs_j, of conj(sign * coef_t) * g_j[j].  The walk
+ * is the forward one (qmb/_hamiltonian_cpu.cpp:80-257) read backwards: every
+ * (term, row i) pair is visited once and the found target's value is pulled
+ * instead of pushed.  Where configs_j repeats a row, its first occurrence
+ * (lowest index) supplies the value, matching the forward map.  Rows
+ * [row_begin, row_end) of configs_i are computed (out_i holds those rows), so
+ * callers can split the rows across processes.
+ */
+void oracle_apply_within_adjoint(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site,
+                                 const uint8_t* kind, const double* coef, int64_t row_begin, int64_t row_end,
+                                 const uint8_t* configs_i, int64_t n_j, const uint8_t* configs_j, const double* g_j,
+                                 double* out_i) {
+    int nq = n_qubytes;
+    int64_t* idx = sorted_index(configs_j, n_j, nq);
+    uint8_t* cur = (uint8_t*)malloc((size_t)nq);
+    int64_t n = row_end - row_begin;
+    memset(out_i, 0, (size_t)(n > 0 ? n : 0) * 2 * sizeof(double));
+    for (int64_t t = 0; t < n_terms; ++t) {
+        for (int64_t i = row_begin; i < row_end; ++i) {
+            memcpy(cur, configs_i + i * nq, (size_t)nq);
+            int parity;
+            if (!oracle_apply_term(nq, particle_cut, site + t * MAX_OPS, kind + t * MAX_OPS, cur, &parity)) {
+                continue;
+            }
+            int64_t pos = find_row(configs_j, idx, n_j, cur, nq);
+            if (pos < 0) {
+                continue;
+            }
+            double sign = parity ? -1.0 : 1.0;
+            const double* c = coef + 2 * t;
+            const double* g = g_j + 2 * idx[pos];
+            /* conj(sign * c) * g */
+            out_i[2 * (i - row_begin) + 0] += sign * (c[0] * g[0] + c[1] * g[1]);
+            out_i[2 * (i - row_begin) + 1] += sign * (c[0] * g[1] - c[1] * g[0]);
+        }
+    }
+    free(cur);
     free(idx);
 }
 
@@ -273,7 +339,12 @@ static int64_t unique_rows(uint8_t* rows, int64_t n, int nq) {
  * Enumerate every candidate record of find_relative in the reference's order
  * (term-major, qmb/_hamiltonian_cpu.cpp:407-440): the image of source i under
  * term t, kept when it is not an excluded row, with weight |sign*coef*psi|^2
- * computed as in :388-392.  mode 0 feeds the heap; mode 1 appends to a list.
+ * computed as in :388-392.  Sources [row_begin, row_end) of configs_i are
+ * walked; a record's visiting order is t * n_i + i with i its index in the
+ * whole configs_i (n_i rows), so that records of row ranges walked
+ * separately rank as one walk would.  Each record goes to the sink: the
+ * reference's heap, a list of every record, a bounded top-K under the ranked
+ * order, or a list of the records of one exact weight.
  */
 typedef struct {
     record_t* list;
@@ -281,15 +352,86 @@ typedef struct {
     int64_t cap;
 } record_list_t;
 
+typedef struct {
+    record_t* heap;       /* the reference's size-heap_n min-heap (heap_offer) */
+    int64_t heap_n;
+    record_list_t* list;  /* every record (or, with filter, the records of weight == filter_weight) */
+    int filter;
+    double filter_weight;
+    record_t* top;        /* bounded min-heap of the top_cap heaviest records under cmp_rank's order */
+    int64_t top_cap;
+    int64_t top_n;
+} record_sink_t;
+
+static void list_push(record_list_t* list, const record_t* rec) {
+    if (list->count == list->cap) {
+        list->cap = list->cap ? list->cap * 2 : 1024;
+        list->list = (record_t*)realloc(list->list, (size_t)list->cap * sizeof(record_t));
+    }
+    list->list[list->count++] = *rec;
+}
+
+/* a ranks below b: lighter, or equally heavy and visited earlier */
+static int rank_below(const record_t* a, const record_t* b) {
+    if (a->weight != b->weight) {
+        return a->weight < b->weight;
+    }
+    return a->order < b->order;
+}
+
+/* Keep the top_cap records that rank highest; the root is the lowest kept. */
+static void top_offer(record_sink_t* s, const record_t* v) {
+    if (v->weight == 0.0) {
+        return; /* the reference drops records of zero weight */
+    }
+    record_t* h = s->top;
+    int64_t pos;
+    if (s->top_n < s->top_cap) {
+        pos = s->top_n++;
+        while (pos > 0) {
+            int64_t up = (pos - 1) / 2;
+            if (!rank_below(v, &h[up])) {
+                break;
+            }
+            h[pos] = h[up];
+            pos = up;
+        }
+        h[pos] = *v;
+        return;
+    }
+    if (!rank_below(&h[0], v)) {
+        return;
+    }
+    int64_t n = s->top_n;
+    pos = 0;
+    for (;;) {
+        int64_t l = 2 * pos + 1, r = l + 1, m = pos;
+        const record_t* low = v;
+        if (l < n && rank_below(&h[l], low)) {
+            m = l;
+            low = &h[l];
+        }
+        if (r < n && rank_below(&h[r], low)) {
+            m = r;
+        }
+        if (m == pos) {
+            break;
+        }
+        h[pos] = h[m];
+        pos = m;
+    }
+    h[pos] = *v;
+}
+
 static void enumerate_candidates(int nq, int particle_cut, int64_t n_terms, const int16_t* site, const uint8_t* kind,
-                                 const double* coef, int64_t n_i, const uint8_t* configs_i, const double* psi_i,
-                                 int64_t n_ex, const uint8_t* configs_ex, record_t* heap, int64_t heap_n,
-                                 record_list_t* list) {
+                                 const double* coef, int64_t n_i, int64_t row_begin, int64_t row_end,
+                                 const uint8_t* configs_i, const double* psi_i, int64_t n_ex,
+                                 const uint8_t* configs_ex, record_sink_t* sink) {
     int64_t* idx = sorted_index(configs_ex, n_ex, nq);
     record_t rec;
     memset(&rec, 0, sizeof(rec));
     for (int64_t t = 0; t < n_terms; ++t) {
-        for (int64_t i = 0; i < n_i; ++i) {
+        for (int64_t i = row_begin; i < row_end; ++i) {
             memcpy(rec.row, configs_i + i * nq, (size_t)nq);
             int parity;
             if (!oracle_apply_term(nq, particle_cut, site + t * MAX_OPS, kind + t * MAX_OPS, rec.row, &parity)) {
@@ -305,15 +447,14 @@ static void enumerate_candidates(int nq, int particle_cut, int64_t n_terms, cons
             double im = sign * (c[0] * p[1] + c[1] * p[0]);
             rec.weight = re * re + im * im;
             rec.order = (uint64_t)t * (uint64_t)n_i + (uint64_t)i;
-            if (heap) {
-                heap_offer(heap, heap_n, &rec);
+            if (sink->heap) {
+                heap_offer(sink->heap, sink->heap_n, &rec);
             }
-            if (list) {
-                if (list->count == list->cap) {
-                    list->cap = list->cap ? list->cap * 2 : 1024;
-                    list->list = (record_t*)realloc(list->list, (size_t)list->cap * sizeof(record_t));
-                }
-                list->list[list->count++] = rec;
+            if (sink->top) {
+                top_offer(sink, &rec);
+            }
+            if (sink->list && (!sink->filter || rec.weight == sink->filter_weight)) {
+                list_push(sink->list, &rec);
             }
         }
     }
@@ -335,8 +476,9 @@ int64_t oracle_find_relative_heap(int n_qubytes, int particle_cut, int64_t n_ter
         return 0;
     }
     record_t* heap = (record_t*)calloc((size_t)count_selected, sizeof(record_t));
-    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, configs_i, psi_i, n_ex, configs_ex, heap,
-                         count_selected, NULL);
+    record_sink_t sink = {heap, count_selected, NULL, 0, 0.0, NULL, 0, 0};
+    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, 0, n_i, configs_i, psi_i, n_ex, configs_ex,
+                         &sink);
     int64_t m = 0;
     for (int64_t k = 0; k < count_selected; ++k) {
         if (heap[k].weight != 0.0) {
@@ -375,8 +517,9 @@ int64_t oracle_find_relative_ranked(int n_qubytes, int particle_cut, int64_t n_t
                                     const uint8_t* configs_ex, uint8_t* out, double* info) {
     int nq = n_qubytes;
     record_list_t list = {NULL, 0, 0};
-    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, configs_i, psi_i, n_ex, configs_ex, NULL, 0,
-                         &list);
+    record_sink_t sink = {NULL, 0, &list, 0, 0.0, NULL, 0, 0};
+    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, 0, n_i, configs_i, psi_i, n_ex, configs_ex,
+                         &sink);
     int64_t nz = 0;
     for (int64_t k = 0; k < list.count; ++k) {
         if (list.list[k].weight != 0.0) {
@@ -413,6 +556,37 @@ int64_t oracle_find_relative_ranked(int n_qubytes, int particle_cut, int64_t n_t
 }
 
 /*
+ * The top_cap records of sources [row_begin, row_end) under the ranked order
+ * of oracle_find_relative_ranked (weight descending, visiting order
+ * descending, zero weights dropped), with visiting orders of the whole
+ * configs_i (n_i rows).  Because the order is total, the top K of a union of
+ * row ranges is the top K of the union of their top-K lists: callers split
+ * the rows across processes and merge.  Writes weights, orders and rows (in
+ * no particular order) and returns the count.
+ */
+int64_t oracle_relative_top_records(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site,
+                                    const uint8_t* kind, const double* coef, int64_t n_i, int64_t row_begin,
+                                    int64_t row_end, const uint8_t* configs_i, const double* psi_i, int64_t top_cap,
+                                    int64_t n_ex, const uint8_t* configs_ex, double* weights, uint64_t* orders,
+                                    uint8_t* rows) {
+    int nq = n_qubytes;
+    if (top_cap <= 0) {
+        return 0;
+    }
+    record_t* top = (record_t*)malloc((size_t)top_cap * sizeof(record_t));
+    record_sink_t sink = {NULL, 0, NULL, 0, 0.0, top, top_cap, 0};
+    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, row_begin, row_end, configs_i, psi_i, n_ex,
+                         configs_ex, &sink);
+    for (int64_t k = 0; k < sink.top_n; ++k) {
+        weights[k] = top[k].weight;
+        orders[k] = top[k].order;
+        memcpy(rows + k * nq, top[k].row, (size_t)nq);
+    }
+    free(top);
+    return sink.top_n;
+}
+
+/*
  * Rows of every candidate whose weight is exactly w (used by the tests to
  * name the boundary-tie class).  Writes up to cap rows, returns the count of
  * distinct rows found.
@@ -423,15 +597,14 @@ int64_t oracle_rows_with_weight(int n_qubytes, int particle_cut, int64_t n_terms
                                 uint8_t* out) {
     int nq = n_qubytes;
     record_list_t list = {NULL, 0, 0};
-    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, configs_i, psi_i, n_ex, configs_ex, NULL, 0,
-                         &list);
+    record_sink_t sink = {NULL, 0, &list, 1, w, NULL, 0, 0};
+    enumerate_candidates(nq, particle_cut, n_terms, site, kind, coef, n_i, 0, n_i, configs_i, psi_i, n_ex, configs_ex,
+                         &sink);
     uint8_t* rows = (uint8_t*)malloc((size_t)(list.count > 0 ? list.count : 1) * (size_t)nq);
     int64_t m = 0;
     for (int64_t k = 0; k < list.count; ++k) {
-        if (list.list[k].weight == w) {
-            memcpy(rows + m * nq, list.list[k].row, (size_t)nq);
-            ++m;
-        }
+        memcpy(rows + m * nq, list.list[k].row, (size_t)nq);
+        ++m;
     }
     int64_t u = unique_rows(rows, m, nq);
     memcpy(out, rows, (size_t)(u < cap ? u : cap) * (size_t)nq);
@@ -502,6 +675,40 @@ void oracle_single_relative(int n_qubytes, int particle_cut, int64_t n_terms, co
         }
     }
     free(kf);
+    free(cur);
+    free(idx);
+}
+
+/*
+ * Columns [col_begin, col_end) of the dense matrix below: mat[j][i - col_begin]
+ * = <j|H|i> for every row j of configs, n x (col_end - col_begin) complex,
+ * row-major.  Callers split the columns across processes.
+ */
+void oracle_dense_columns(int n_qubytes, int particle_cut, int64_t n_terms, const int16_t* site, const uint8_t* kind,
+                          const double* coef, int64_t n, const uint8_t* configs, int64_t col_begin, int64_t col_end,
+                          double* mat) {
+    int nq = n_qubytes;
+    int64_t w = col_end - col_begin;
+    int64_t* idx = sorted_index(configs, n, nq);
+    uint8_t* cur = (uint8_t*)malloc((size_t)nq);
+    memset(mat, 0, (size_t)n * (size_t)(w > 0 ? w : 0) * 2 * sizeof(double));
+    for (int64_t t = 0; t < n_terms; ++t) {
+        for (int64_t i = col_begin; i < col_end; ++i) {
+            memcpy(cur, configs + i * nq, (size_t)nq);
+            int parity;
+            if (!oracle_apply_term(nq, particle_cut, site + t * MAX_OPS, kind + t * MAX_OPS, cur, &parity)) {
+                continue;
+            }
+            int64_t pos = find_row(configs, idx, n, cur, nq);
+            if (pos < 0) {
+                continue;
+            }
+            int64_t j = idx[pos];
+            double sign = parity ? -1.0 : 1.0;
+            mat[2 * (j * w + (i - col_begin)) + 0] += sign * coef[2 * t + 0];
+            mat[2 * (j * w + (i - col_begin)) + 1] += sign * coef[2 * t + 1];
+        }
+    }
     free(cur);
     free(idx);
 }

@@ -45,13 +45,14 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_diagonal_term": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P]),
     "qmbx_find_relative_workspace": (ctypes.c_int, [_P, _I64, _I64, _I64, _PU64]),
     "qmbx_find_relative": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _I64, _P, _PI64, _P, _U64, _PU64, _P]),
+    "qmbx_find_relative_stats": (ctypes.c_int, [_PI64]),
     "qmbx_single_relative_workspace": (ctypes.c_int, [_P, _I64, _PU64]),
     "qmbx_single_relative": (ctypes.c_int, [_P, _P, _P, _I64, _U64, _P, _P, _U64, _P]),
     "qmbx_profile_enable": (ctypes.c_int, [_I32]),
     "qmbx_profile_read": (ctypes.c_int, [_PI64, _PI64, ctypes.POINTER(ctypes.c_double)]),
 }
 
-PROFILE_GROUPS = ("enumerate", "keys", "select", "other", "diagonal")
+PROFILE_GROUPS = ("enumerate", "keys", "select", "other", "diagonal", "sort")
 
 
 def profile_enable(on: bool) -> None:
@@ -67,6 +68,16 @@ def profile_read() -> dict:
     check(library().qmbx_profile_read(ctypes.byref(launches), counts, ms))
     return {"launches": launches.value,
             "groups": {g: (counts[k], ms[k]) for k, g in enumerate(PROFILE_GROUPS)}}
+
+
+FIND_STATS = ("records", "walks", "sort_passes", "sort_bytes", "selected", "rows_out")
+
+
+def find_relative_stats() -> dict:
+    """Figures of this thread's last find_relative call (see qmbx_find_relative_stats)."""
+    vals = (ctypes.c_int64 * len(FIND_STATS))()
+    check(library().qmbx_find_relative_stats(vals))
+    return dict(zip(FIND_STATS, list(vals)))
 
 
 class QmbxError(RuntimeError):

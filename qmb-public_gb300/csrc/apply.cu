@@ -665,14 +665,15 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     PartView diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     const bool include_diag = a.prec == Prec::F64 || a.include_diag;
     if (!include_diag) diag.n = 0;
-    const bool scatter = !a.same && 2 * n_in < n_out;
+    const bool exact_order = deterministic_mode();
+    const bool scatter = !exact_order && !a.same && 2 * n_in < n_out;
     // walk the input side (scatter) with forward terms for the forward map
     // or daggered terms (conjugated) for the adjoint; walk the output side
     // (gather) with daggered terms for the forward map or forward terms
     // (conjugated) for the adjoint
     const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
     const HashRows& walk = scatter ? in_set : out_set;
-    const Walk kind = choose_walk(part, walk.n, true);
+    const Walk kind = choose_walk(part, walk.n, !exact_order);
     const bool pivot = kind == Walk::kPivot;
     if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashView look = scatter ? out_set.hash() : in_set.hash();

@@ -934,6 +934,13 @@ constexpr int64_t kFewWideRows = 65536;
 enum class Walk { kTiled, kGrouped, kPivot };
 Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok);
 
+// QMBX_DETERMINISTIC=1 in the environment (read at every call): apply_within
+// and its adjoint take only walks whose sums have a fixed order (the gather
+// direction, no pivot-major walk), so that repeated calls give identical
+// bits.  The scatter and pivot walks add into their outputs with FP64
+// atomics, whose order varies from run to run.
+bool deterministic_mode();
+
 // Grid for grouped_kernel: enough warps for every row, at most a few waves.
 int grouped_grid(int64_t n_rows);
 
@@ -1041,6 +1048,7 @@ struct UniqueRows {
 // Exclusive prefix sum of n int32 values (in == out allowed); the total goes
 // to *total when non-NULL.  scratch holds scan_scratch(n) int32 values.
 int64_t scan_scratch(int64_t n);
-int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s);
+int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s,
+                   int group = kGroupKeys);
 
 }  // namespace qmbx

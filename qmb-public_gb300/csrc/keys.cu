@@ -165,12 +165,13 @@ int64_t scan_scratch(int64_t n) {
     return nb < 1 ? 1 : nb;
 }
 
-int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s) {
+int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s,
+                   int group) {
     int64_t nb = scan_scratch(n);
-    if (n > 0) QMBX_KERNEL(kGroupKeys, s, scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch));
-    else QMBX_KERNEL(kGroupKeys, s, set_zero_kernel<<<1, 1, 0, s>>>(scratch));
-    QMBX_KERNEL(kGroupKeys, s, scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total));
-    if (n > 0) QMBX_KERNEL(kGroupKeys, s, scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, scratch));
+    if (n > 0) QMBX_KERNEL(group, s, scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch));
+    else QMBX_KERNEL(group, s, set_zero_kernel<<<1, 1, 0, s>>>(scratch));
+    QMBX_KERNEL(group, s, scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total));
+    if (n > 0) QMBX_KERNEL(group, s, scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, scratch));
     QMBX_LAUNCH_CHECK("exclusive_scan");
     return QMBX_OK;
 }
@@ -308,10 +309,10 @@ int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_o
         bool to_out = ((n_bytes - 1 - p) & 1) == 0;
         uint64_t* dst_k = to_out ? keys_out : sc.keys;
         int32_t* dst_v = to_out ? vals_out : sc.vals;
-        QMBX_KERNEL(kGroupKeys, s, radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
-        int st = exclusive_scan(sc.counts, sc.counts, (int64_t)256 * nblocks, nullptr, sc.scan, s);
+        QMBX_KERNEL(kGroupSort, s, radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
+        int st = exclusive_scan(sc.counts, sc.counts, (int64_t)256 * nblocks, nullptr, sc.scan, s, kGroupSort);
         if (st != QMBX_OK) return st;
-        QMBX_KERNEL(kGroupKeys, s, radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
+        QMBX_KERNEL(kGroupSort, s, radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
                                                                  nblocks));
         QMBX_LAUNCH_CHECK("radix sort pass");
         src_k = dst_k;
@@ -571,6 +572,11 @@ Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok) {
         return pivot_ok && big_groups ? Walk::kPivot : Walk::kGrouped;
     }
     return n_rows < (part.wide ? kFewWideRows : kFewRows) ? Walk::kGrouped : Walk::kTiled;
+}
+
+bool deterministic_mode() {
+    const char* e = getenv("QMBX_DETERMINISTIC");
+    return e != nullptr && e[0] != 0 && e[0] != '0';
 }
 
 int grouped_grid(int64_t n_rows) {

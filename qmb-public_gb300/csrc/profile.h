@@ -6,14 +6,16 @@
 namespace qmbx {
 
 // kGroupEnumerate is the main term walk; kGroupDiagonal the separate
-// passes over diagonal terms that follow it
+// passes over diagonal terms that follow it; kGroupSort the radix sorts
+// (histogram, scan and scatter passes)
 enum ProfileGroup {
     kGroupEnumerate = 0,
     kGroupKeys = 1,
     kGroupSelect = 2,
     kGroupOther = 3,
     kGroupDiagonal = 4,
-    kProfileGroups = 5
+    kGroupSort = 5,
+    kProfileGroups = 6
 };
 
 void note_launch(int n);

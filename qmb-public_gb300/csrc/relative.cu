@@ -33,6 +33,17 @@ namespace {
 
 constexpr int kBuckets = 4096;
 
+// Figures of the calling thread's last find_relative call (qmbx_find_relative_stats).
+struct FindStats {
+    int64_t records;      // records emitted by the selection pass
+    int64_t walks;        // term walks run (histogram and emission passes)
+    int64_t sort_passes;  // radix passes over records and selected rows
+    int64_t sort_bytes;   // passes x 2 (read + write) x items x item bytes
+    int64_t selected;     // records selected before de-duplication
+    int64_t rows_out;     // distinct rows returned
+};
+thread_local FindStats g_find_stats{};
+
 __device__ __forceinline__ int weight_bucket(float est) {
     // 0 for zero (or underflowed) estimates; otherwise 1 + the top 12 bits of
     // the IEEE pattern, which is monotone for non-negative floats
@@ -325,6 +336,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
                     (unsigned long long)ws.used);
     }
     *a.n_out = 0;
+    g_find_stats = FindStats{};
     if (k == 0 || a.n_i == 0) return QMBX_OK;
     int st;
     if ((st = build_hashrows<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
@@ -369,6 +381,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         rs.psi = L.psi_s;
         rs.n_i = n_s;
         if ((st = launch_relative<W, false>(rs, L.keys_s, n_s, s)) != QMBX_OK) return st;
+        ++g_find_stats.walks;
         if ((st = read_hist()) != QMBX_OK) return st;
         // aim at about twice k records above the chosen bucket, one more bucket of slack
         const int b_est = bucket_above(hist, (double)a.n_i / (double)n_s, 2.0 * (double)k);
@@ -382,6 +395,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
     } else {
         if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
+        ++g_find_stats.walks;
         if ((st = read_hist()) != QMBX_OK) return st;
         const int b_k = bucket_above(hist, 1.0, (double)k);
         emit_from = b_k > 1 ? b_k - 1 : 0;
@@ -405,6 +419,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     for (int attempt = 0;; ++attempt) {
         r.emit_from = emit_from;
         if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
+        ++g_find_stats.walks;
         int overflow = 0;
         QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
         QMBX_CUDA_TRY(cudaMemcpyAsync(&overflow, L.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -430,6 +445,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
         QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
     }
+    g_find_stats.records = (int64_t)n_emit;
     if (n_emit == 0) return QMBX_OK;
     const int64_t e = (int64_t)n_emit;
     QMBX_CUDA_TRY(cudaMemsetAsync(L.n_zero, 0, sizeof(unsigned long long), s));
@@ -452,6 +468,10 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     const int64_t valid = e - (int64_t)n_zero;
     if (valid <= 0) return QMBX_OK;
     const int64_t keep = valid < k ? valid : k;
+    // rank keys of 16 bytes + 4-byte record index per item; selected rows of 8W bytes + 4-byte index
+    g_find_stats.selected = keep;
+    g_find_stats.sort_passes = (8 + order_bytes) + nq;
+    g_find_stats.sort_bytes = (int64_t)(8 + order_bytes) * 2 * e * (16 + 4) + (int64_t)nq * 2 * keep * (8 * W + 4);
     QMBX_KERNEL(kGroupSelect, s, gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
                                                                             L.sel_keys));
     QMBX_LAUNCH_CHECK("gather_selected_kernel");
@@ -466,6 +486,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     if ((st = unpack_rows<W>(L.final_set.keys, nullptr, n_unique, nq, a.out, s)) != QMBX_OK) return st;
     QMBX_CUDA_TRY(cudaStreamSynchronize(s));
     *a.n_out = n_unique;
+    g_find_stats.rows_out = n_unique;
     return QMBX_OK;
 }
 
@@ -660,6 +681,19 @@ extern "C" int qmbx_find_relative(const void* table_host, const void* table_dev,
         case 4: return find_impl<4>(a, workspace, workspace_bytes, workspace_needed, s);
         default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
     }
+}
+
+extern "C" int qmbx_find_relative_stats(int64_t stats[6]) {
+    clear_error();
+    if (stats == nullptr) return fail(QMBX_ERR_ARGUMENT, "stats must not be NULL");
+    const FindStats& f = g_find_stats;
+    stats[0] = f.records;
+    stats[1] = f.walks;
+    stats[2] = f.sort_passes;
+    stats[3] = f.sort_bytes;
+    stats[4] = f.selected;
+    stats[5] = f.rows_out;
+    return QMBX_OK;
 }
 
 extern "C" int qmbx_single_relative_workspace(const void* table_host, int64_t n, uint64_t* bytes) {

@@ -44,11 +44,18 @@ class _HermitianEnergy(torch.autograd.Function):
         return None, None, g.to(ctx.in_dtype)
 
 
-def variational_energy(ham: Hamiltonian, configs: torch.Tensor, psi: torch.Tensor) -> torch.Tensor:
-    """Re<psi|H|psi> / <psi|psi> over one set of configurations; a float64 scalar."""
+def variational_energy(ham: Hamiltonian, configs: torch.Tensor, psi: torch.Tensor, *,
+                       hermitian_shortcut: bool = True) -> torch.Tensor:
+    """Re<psi|H|psi> / <psi|psi> over one set of configurations; a float64 scalar.
+
+    With ``hermitian_shortcut`` (the default) a Hermitian operator takes its
+    gradient from the saved H psi; ``hermitian_shortcut=False`` always sends
+    the backward pass through the adjoint kernel (``apply_within``'s autograd
+    function), which the gradient checks use to exercise that kernel.
+    """
     if psi.dtype not in (torch.complex64, torch.complex128):
         raise RuntimeError("psi must be complex64 or complex128")
-    if psi.requires_grad and torch.is_grad_enabled() and configs.dim() == 2 and \
+    if hermitian_shortcut and psi.requires_grad and torch.is_grad_enabled() and configs.dim() == 2 and \
             ham._table(configs.device, configs.shape[1]).hermitian:
         return _HermitianEnergy.apply(ham, configs, psi)
     if psi.dtype == torch.complex64:

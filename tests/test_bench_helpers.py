@@ -1,7 +1,15 @@
 """Host-side pieces of bench.py: the clock record, the figures read from the
-committed ncu summaries, the replica arithmetic and the workload generators."""
+committed ncu summaries (used only on the kernel sources they were taken
+on), the reference arm's timing, the replica arithmetic and the workload
+generators."""
 
 from __future__ import annotations
+
+import argparse
+import glob
+import json
+import os
+import time
 
 import numpy as np
 
@@ -22,12 +30,47 @@ def test_clock_summary_flags_throttling():
     assert out["reasons"] == ["hw_slowdown", "sw_power_cap"]
 
 
-def test_committed_profile_figures_are_readable():
-    # the bench line's traffic and issue roofline come from these summaries
-    assert bench.ncu_traffic("c2") > 1e6
-    inst = bench.ncu_figure("c2", "warp_instructions_per_launch")
-    assert inst is not None and inst > 1e8
-    assert bench.ncu_traffic("no-such-workload") is None
+def test_committed_profile_figures_are_keyed_to_the_kernel_sources(tmp_path, monkeypatch):
+    # a figure is used only when taken on the current kernel sources
+    sha = bench.kernel_sources_sha()
+    assert len(sha) == 16
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    (prof / "fresh.json").write_text(json.dumps({"kernel_sources_sha": sha, "warp_instructions_per_launch": 5e8}))
+    (prof / "stale.json").write_text(json.dumps({"kernel_sources_sha": "0" * 16, "warp_instructions_per_launch": 5e8}))
+    for rel in bench.KERNEL_SOURCES:
+        (tmp_path / rel).parent.mkdir(parents=True, exist_ok=True)
+        (tmp_path / rel).write_bytes(open(os.path.join(bench.REPO, rel), "rb").read())
+    monkeypatch.setattr(bench, "REPO", str(tmp_path))
+    assert bench.ncu_figures("fresh")["warp_instructions_per_launch"] == 5e8
+    assert bench.ncu_figures("stale") is None
+    assert bench.ncu_figures("absent") is None
+
+
+def test_committed_profile_json_files_parse():
+    for path in glob.glob(os.path.join(bench.REPO, "profiles", "*.json")):
+        figs = json.load(open(path))
+        assert len(figs["kernel_sources_sha"]) == 16 and "command" in figs, path
+
+
+def test_both_arms_report_the_same_config():
+    wl = bench.make_workload("c1")
+    args = argparse.Namespace(workload="c1", gpus=1)
+    assert bench.workload_config(args, wl) == bench.workload_config(args, wl)
+    assert bench.workload_config(args, wl)["n_i"] == 400
+
+
+def test_reference_arm_times_what_it_reports():
+    # a tiny fraction of C1 on two processes: the line's steps and times are the ones it ran
+    wl = bench.make_workload("c1")
+    args = argparse.Namespace(workload="c1", gpus=1, steps=3, warmup=1, ref_fraction=0.1)
+    t0 = time.perf_counter()
+    line = bench.run_reference(args, wl)
+    wall = time.perf_counter() - t0
+    assert line["impl"] == "reference" and line["steps"] == 3
+    assert line["ms_per_step"] * line["steps"] / 1e3 <= wall
+    assert line["value"] > 0 and line["cpu_baseline"]["one_core"]["cores"] == 1
+    assert line["config"] == bench.workload_config(args, wl)
 
 
 def test_replica_value_and_single_rank_max():
