@@ -579,7 +579,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     value = replica_value(units, ms_step32, world)
     # the radix sorts of find_relative: passes x 2 x records x record bytes over their device time
     n_sort, ms_sort = prof_rel["groups"]["sort"]
-    sort_bytes = reps * stats_rel["sort_bytes"]
+    sort_bytes = stats_rel["sort_bytes"]  # per call; ms_sort covers `reps` calls
     line = {
         "metric": "apply_within term-applications/s (FP32-compensated forward + adjoint)",
         "value": value,
@@ -610,8 +610,9 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
         "find_relative": {"ms": ms_rel, "count_selected": K, "rows_out": int(rel.shape[0]),
                           "kernel_groups_ms": {g: prof_rel["groups"][g][1] / reps for g in prof_rel["groups"]},
                           "stats": stats_rel,
-                          "sort_roofline": hbm_roofline(sort_bytes, ms_sort, "radix sorts (radix_hist/scatter + scans)",
-                                                        None, launches=n_sort) if ms_sort > 0 else None},
+                          "sort_roofline": hbm_roofline(sort_bytes, ms_sort / reps,
+                                                        "radix sort of the selected rows (radix_hist/scatter + scans)",
+                                                        None, launches_per_call=n_sort / reps) if ms_sort > 0 else None},
         "energy": {"fp64": e64, "fp32c": e32, "abs_error_ha": abs(e32 - e64)},
         "kernel_groups_ms_per_step": {g: prof["groups"][g][1] / args.steps for g in prof["groups"]},
         "clock_window": "nvidia-smi every 50 ms across the FP32c, FP64, find_relative and end-to-end timed loops",
@@ -829,8 +830,8 @@ def run_extra(args, wl) -> dict:
                      "rows_out": int(rel.shape[0]), "term_applications_per_s": T * n / (ms * 1e-3),
                      "stats": stats,
                      "roofline": walk_roofline(prof, n, ci.shape[0], 16, "term walk (pivot_kernel)"),
-                     "sort_roofline": hbm_roofline(stats["sort_bytes"], ms_sort, "radix sorts", None,
-                                                   launches=n_sort) if ms_sort > 0 else None,
+                     "sort_roofline": hbm_roofline(stats["sort_bytes"], ms_sort, "radix sort of the selected rows",
+                                                   None, launches_per_call=n_sort) if ms_sort > 0 else None,
                      "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
     line["clocks"] = clocks.summary()
     return line

@@ -108,11 +108,14 @@ int qmbx_apply_within(const void* table_host, const void* table_dev, const uint8
  * scratch is a fixed device array of QMBX_STATIC_SCRATCH_BYTES inside this
  * library, which every GPU that loads the library holds until the process
  * exits.  Inputs needing more scratch than that (qmbx_apply_within_workspace)
- * are rejected with QMBX_ERR_ARGUMENT.  The array's device address is looked
- * up on the first call made on each device (with that device current), so
- * make that first call before any stream capture.  All calls share the one
- * array: calls whose work overlaps on the GPU race and must be serialised by
- * the caller.  Calls no allocation routine.
+ * are rejected with QMBX_ERR_ARGUMENT; a same_configs call is sized for its
+ * one row set.  The array's device address is looked up with the calling
+ * device current, on every call made on a stream that is not capturing (so a
+ * device reset leaves no stale address); a call on a capturing stream uses
+ * the address of the last call on that device, so make the first call on
+ * each device before any stream capture.  All calls share the one array:
+ * calls whose work overlaps on the GPU race and must be serialised by the
+ * caller.  Calls no allocation routine.
  */
 #define QMBX_STATIC_SCRATCH_BYTES (32ull << 20)
 

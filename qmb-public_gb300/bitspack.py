@@ -3,8 +3,10 @@
 Configurations reach the engine packed by ``pack_int(bits, 1)``: element e of
 the last dimension lands in byte e // 8 at bit e % 8, least significant bit
 first, and the last byte is zero-padded.  The engine's kernels rely on exactly
-this layout: a little-endian 64-bit load of a row holds site s at bit s % 64
-of word s // 64.
+this layout: they read a row as big-endian 64-bit key words (row byte b in
+word b // 8 at bits (7 - b % 8) * 8 .. +7), so that comparing words as
+unsigned integers is the reference's lexicographic byte order, and site s
+sits in word s // 64 at bit (7 - (s // 8) % 8) * 8 + s % 8.
 """
 
 from __future__ import annotations

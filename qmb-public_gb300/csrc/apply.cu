@@ -837,17 +837,19 @@ int diagonal_impl(const void* table_host, const void* table_dev, const uint8_t* 
 
 using namespace qmbx;
 
-extern "C" int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, int64_t n_j, uint64_t* bytes) {
-    clear_error();
-    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+namespace qmbx {
+
+// Workspace of an apply_within call on n_i x n_j rows, for one value of
+// same_configs (one row set instead of two when it is set): the largest of
+// the forward / adjoint, FP64 / FP32 layouts (they differ by one value array).
+int apply_within_workspace_for(const void* table_host, int64_t n_i, int64_t n_j, bool same, uint64_t* bytes) {
     const qmbx_table_header* h = header_of(table_host);
     if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
-    // the largest of the forward / adjoint, FP64 / FP32 layouts (they differ by one value array)
     ApplyArgs a{};
     a.table_host = table_host;
     a.n_i = n_i;
-    a.n_j = n_j;
-    a.same = false;
+    a.n_j = same ? n_i : n_j;
+    a.same = same;
     a.prec = Prec::F64;
     uint64_t most = 0;
     for (int adj = 0; adj < 2; ++adj) {
@@ -859,6 +861,15 @@ extern "C" int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, 
     }
     *bytes = most;
     return QMBX_OK;
+}
+
+}  // namespace qmbx
+
+extern "C" int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, int64_t n_j, uint64_t* bytes) {
+    clear_error();
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    // sized for two row sets, which also covers same_configs calls
+    return apply_within_workspace_for(table_host, n_i, n_j, false, bytes);
 }
 
 extern "C" int qmbx_apply_within(const void* table_host, const void* table_dev, const uint8_t* configs_i,

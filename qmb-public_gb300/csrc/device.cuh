@@ -247,6 +247,9 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
 
 int check_table(const void* table_host, const void* table_dev);
 
+// Workspace of an apply_within call for one value of same_configs (apply.cu).
+int apply_within_workspace_for(const void* table_host, int64_t n_i, int64_t n_j, bool same, uint64_t* bytes);
+
 // ---------------------------------------------------------------------------
 // the enumeration kernel: every (configuration, term) pair of one or two
 // table parts, terms staged through shared memory tile by tile so that all
@@ -1007,6 +1010,11 @@ RowSet take_rowset(Arena& ws, int64_t n);
 
 template <int W>
 int build_rowset(const uint8_t* rows, int n_qubytes, RowSet& out, cudaStream_t s);
+
+// Sort out.n keys by their first n_bytes row bytes and keep the distinct ones
+// (out.keys[0 .. *out.count)); builds no hash set.
+template <int W>
+int sort_unique_keys(const uint64_t* keys, int n_bytes, RowSet& out, cudaStream_t s);
 
 // A de-duplicated row set without sorting: every row's key is inserted in an
 // open-addressing hash set whose entries name the first (lowest) row holding

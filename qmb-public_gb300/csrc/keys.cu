@@ -160,6 +160,30 @@ __global__ void scan_apply_kernel(const int32_t* __restrict__ in, int32_t* __res
     }
 }
 
+// Exclusive scan of up to kScanChunk values in one block (one launch instead of three).
+__global__ void scan_single_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                                   int* __restrict__ total_out) {
+    __shared__ int32_t s_warp[32];
+    const int64_t base = (int64_t)threadIdx.x * kScanItems;
+    int32_t v[kScanItems];
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        local += v[k];
+    }
+    int32_t total;
+    int32_t run = block_exclusive_scan(local, s_warp, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = total;
+}
+
 int64_t scan_scratch(int64_t n) {
     int64_t nb = (n + kScanChunk - 1) / kScanChunk;
     return nb < 1 ? 1 : nb;
@@ -168,6 +192,11 @@ int64_t scan_scratch(int64_t n) {
 int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32_t* scratch, cudaStream_t s,
                    int group) {
     int64_t nb = scan_scratch(n);
+    if (n > 0 && n <= kScanChunk) {
+        QMBX_KERNEL(group, s, scan_single_kernel<<<1, kScanThreads, 0, s>>>(in, out, n, total));
+        QMBX_LAUNCH_CHECK("exclusive_scan");
+        return QMBX_OK;
+    }
     if (n > 0) QMBX_KERNEL(group, s, scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, scratch));
     else QMBX_KERNEL(group, s, set_zero_kernel<<<1, 1, 0, s>>>(scratch));
     QMBX_KERNEL(group, s, scan_sums_kernel<<<1, kScanThreads, 0, s>>>(scratch, nb, total));
@@ -425,6 +454,27 @@ int build_rowset(const uint8_t* rows, int nq, RowSet& out, cudaStream_t s) {
     return QMBX_OK;
 }
 
+// Sort out.n keys (W words, first n_bytes row bytes significant) and keep
+// the distinct ones: out.keys[0 .. *out.count) in lexicographic order.  The
+// keys are copied first, so `keys` may be any buffer; no hash set is built.
+template <int W>
+int sort_unique_keys(const uint64_t* keys, int n_bytes, RowSet& out, cudaStream_t s) {
+    const int64_t n = out.n;
+    if (n == 0) {
+        QMBX_KERNEL(kGroupKeys, s, set_int_kernel<<<1, 1, 0, s>>>(out.count, 0));
+        QMBX_LAUNCH_CHECK("set_int_kernel");
+        return QMBX_OK;
+    }
+    int st;
+    if ((st = sort_pairs<W>(keys, nullptr, out.sorted_keys, out.perm, n, n_bytes, out.sort, s)) != QMBX_OK) return st;
+    QMBX_KERNEL(kGroupKeys, s, head_flags_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, n, out.head));
+    if ((st = exclusive_scan(out.head, out.pos, n, nullptr, out.sort.scan, s)) != QMBX_OK) return st;
+    QMBX_KERNEL(kGroupKeys, s, compact_heads_kernel<W><<<grid_for(n, kThreads), kThreads, 0, s>>>(out.sorted_keys, out.perm, out.head, out.pos, n,
+                                                                       out.keys, out.first, out.start, out.count));
+    QMBX_LAUNCH_CHECK("sort_unique_keys");
+    return QMBX_OK;
+}
+
 // ---------------------------------------------------------------------------
 // hash-based de-duplicated row sets
 // ---------------------------------------------------------------------------
@@ -534,6 +584,7 @@ int build_hashrows(const uint8_t* rows, int nq, HashRows& out, cudaStream_t s) {
                                const SortScratch&, cudaStream_t);                                               \
     template RowSet take_rowset<W>(Arena&, int64_t);                                                            \
     template int build_rowset<W>(const uint8_t*, int, RowSet&, cudaStream_t);                                   \
+    template int sort_unique_keys<W>(const uint64_t*, int, RowSet&, cudaStream_t);                              \
     template HashRows take_hashrows<W>(Arena&, int64_t);                                                        \
     template int build_hashrows<W>(const uint8_t*, int, HashRows&, cudaStream_t);
 

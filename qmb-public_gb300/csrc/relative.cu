@@ -7,24 +7,25 @@
 //
 //   find_relative  pass 1 counts the candidate records per weight bucket (the
 //                  top 12 bits of an FP32 estimate |coef|^2 |psi|^2 of the
-//                  weight) over every 16th source row; the host picks from
-//                  the scaled counts a bucket that should hold about twice
+//                  weight) over every 16th source row (every row of small
+//                  inputs); one warp on the device picks from the scaled
+//                  counts a bucket that should hold about twice
 //                  count_selected records above it; pass 2 enumerates every
 //                  row, counts all records per bucket and keeps those at or
-//                  above the bucket below the chosen one, now with the exact
-//                  FP64 weight of the reference (:494-497).  The exact counts
-//                  of pass 2 then confirm that every record down to the
+//                  above the bucket below the chosen one.  The exact counts
+//                  of pass 2 confirm that every record down to the
 //                  count_selected-th was kept (else pass 2 runs again with
-//                  the exact threshold); a radix sort ranks the kept records
-//                  by (weight, visiting order) and the first count_selected
-//                  are sorted and de-duplicated by row.  Small inputs count
-//                  every row in pass 1 and need no confirmation.
+//                  the exact threshold) -- the one host round trip before
+//                  the result.  The kept records get the reference's exact
+//                  FP64 weight (:494-497) and a 128-bit rank key (weight,
+//                  visiting order); a radix select over 12-bit digits finds
+//                  the count_selected-th key, the records up to it are
+//                  compacted, and their rows are sorted and de-duplicated.
 //   single_relative  one thread per row keeps the best Efraimidis-Spirakis
 //                  key of its candidates in registers.
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <vector>
 
 #include "device.cuh"
 
@@ -62,6 +63,25 @@ __device__ __forceinline__ double exact_weight(double2 cf, double2 p, int parity
     return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
 }
 
+// Device-side state of one find_relative call: the selection threshold of
+// the emission pass, its confirmation, and the radix select of the kept
+// records.  Read by the host once, after the emission pass.
+struct FindCtl {
+    unsigned long long n_emit;     // records emitted (atomic counter of the emission pass)
+    unsigned long long n_zero;     // emitted records of zero exact weight
+    unsigned long long need;       // records at or above min(emit_from, exact_from) (emission pass counts)
+    unsigned long long sel_p0;     // radix select: key prefix chosen so far (128 bits, MSB aligned)
+    unsigned long long sel_p1;
+    unsigned long long n_sel;      // records accepted by the compaction
+    long long sel_need;            // records still to accept below the prefix
+    int overflow;
+    int emit_from;                 // lowest bucket the emission pass keeps
+    int exact_from;                // the same choice from the emission pass's full counts
+    int sel_bits;                  // key bits fixed so far
+    int sel_done;
+    int pad;
+};
+
 // The histogram (EMIT = false) and emission (EMIT = true) passes as
 // visitors of the enumeration kernels.  Every (term, row) image that is not
 // an excluded row is a candidate record; diagonal terms produce the row
@@ -73,14 +93,12 @@ struct RelativeArgs {
     PartView off, diag;
     // pass 1
     unsigned long long* hist;
-    // pass 2
-    int emit_from;           // lowest bucket emitted
-    unsigned long long* n_emit;
+    // pass 2 (emit_from, the record counter and the overflow flag live in ctl)
+    FindCtl* ctl;
     int64_t cap_emit;
     uint64_t* emit_rank;     // [cap][2]: (slot | part << 62 | parity << 63, row) from the walk;
                              // (~weight bits, ~order) after rank_records_kernel
     uint64_t* emit_keys;     // [cap][W]
-    int* overflow;
 };
 
 template <int W, bool EMIT>
@@ -122,10 +140,10 @@ struct RelativeVisitor : VisitorBase {
         const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
         atomicAdd(&acc.hist[b], 1);
         if (!EMIT) return;
-        if (b < a.emit_from) return;
-        const unsigned long long at = atomicAdd(a.n_emit, 1ull);
+        if (b < a.ctl->emit_from) return;
+        const unsigned long long at = atomicAdd(&a.ctl->n_emit, 1ull);
         if ((int64_t)at >= a.cap_emit) {
-            *a.overflow = 1;
+            a.ctl->overflow = 1;
             return;
         }
         a.emit_rank[2 * at + 0] = (uint64_t)slot | ((uint64_t)part << 62) | ((uint64_t)parity << 63);
@@ -199,17 +217,6 @@ __global__ void rank_records_kernel(uint64_t* __restrict__ rank, int64_t n, Part
     rank[2 * i + 1] = (~order) << order_shift;
 }
 
-// Gather the keys of the first `keep` ranked records.
-template <int W>
-__global__ void gather_selected_kernel(const int32_t* __restrict__ order, const uint64_t* __restrict__ keys,
-                                       int64_t keep, uint64_t* __restrict__ out) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= keep) return;
-    int64_t src = order[i];
-#pragma unroll
-    for (int q = 0; q < W; ++q) out[i * W + q] = keys[src * W + q];
-}
-
 // Inputs of 4,096 rows or more count records on every kSampleStride-th row
 // in pass 1.
 constexpr int64_t kSampleStride = 16;
@@ -227,16 +234,241 @@ __global__ void sample_rows_kernel(const uint64_t* __restrict__ keys, const doub
     psi_s[j] = psi[r];
 }
 
-// Highest bucket b whose buckets >= b hold at least `target` records
-// (counts scaled by `scale`): the bucket of the target-th heaviest record;
-// 0 when all buckets above 0 hold fewer.
-int bucket_above(const std::vector<unsigned long long>& hist, double scale, double target) {
-    double above = 0.0;
-    for (int b = kBuckets - 1; b >= 1; --b) {
-        above += scale * (double)hist[b];
-        if (above >= target) return b;
+// emit_from from the counts of pass 1 (scaled by `scale`): one bucket below
+// the highest bucket b whose buckets >= b hold at least `target` records (0
+// when all buckets above 0 hold fewer); then the counts are cleared for the
+// emission pass.  One warp: lane l sums the 128 buckets [4096 - 128(l + 1),
+// 4096 - 128 l), a suffix scan over the lanes finds the lane where the
+// running count reaches the target, and that lane walks its buckets.
+__global__ void choose_emit_kernel(unsigned long long* __restrict__ hist, double scale, double target,
+                                   FindCtl* __restrict__ ctl) {
+    const int lane = threadIdx.x;
+    constexpr int kPer = kBuckets / 32;
+    const int hi = kBuckets - kPer * lane;  // lane covers buckets [hi - kPer, hi)
+    double mine = 0.0;
+    for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) mine += scale * (double)hist[b];
+    // inclusive scan from the top lanes down (lane 0 holds the highest buckets)
+    double run = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, run, d);
+        if (lane >= d) run += y;
     }
-    return 0;
+    const unsigned crossed = __ballot_sync(0xffffffffu, run >= target);
+    int b_k = 0;
+    if (crossed) {
+        const int first = __ffs(crossed) - 1;
+        if (lane == first) {
+            double above = run - mine;
+            for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) {
+                above += scale * (double)hist[b];
+                if (above >= target) {
+                    b_k = b;
+                    break;
+                }
+            }
+        }
+        b_k = __shfl_sync(0xffffffffu, b_k, first);
+    }
+    __syncwarp();
+    for (int b = lane; b < kBuckets; b += 32) hist[b] = 0;
+    if (lane == 0) ctl->emit_from = b_k > 1 ? b_k - 1 : 0;
+}
+
+// After the emission pass: the exact threshold from its full counts, and the
+// records needed to hold every record down to the k-th.
+__global__ void check_emit_kernel(const unsigned long long* __restrict__ hist, double k, FindCtl* __restrict__ ctl) {
+    const int lane = threadIdx.x;
+    constexpr int kPer = kBuckets / 32;
+    const int hi = kBuckets - kPer * lane;
+    unsigned long long mine = 0;
+    for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) mine += hist[b];
+    unsigned long long run = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, run, d);
+        if (lane >= d) run += y;
+    }
+    const unsigned crossed = __ballot_sync(0xffffffffu, (double)run >= k);
+    int b_k = 0;
+    if (crossed) {
+        const int first = __ffs(crossed) - 1;
+        if (lane == first) {
+            unsigned long long above = run - mine;
+            for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) {
+                above += hist[b];
+                if ((double)above >= k) {
+                    b_k = b;
+                    break;
+                }
+            }
+        }
+        b_k = __shfl_sync(0xffffffffu, b_k, first);
+    }
+    const int exact_from = b_k > 1 ? b_k - 1 : 0;
+    const int from = exact_from < ctl->emit_from ? exact_from : ctl->emit_from;
+    unsigned long long need = 0;
+    for (int b = lane; b < kBuckets; b += 32) need += b >= from ? hist[b] : 0ull;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) need += __shfl_xor_sync(0xffffffffu, need, d);
+    if (lane == 0) {
+        ctl->exact_from = exact_from;
+        ctl->need = need;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// radix select of the count_selected smallest rank keys (128 bits: ~weight,
+// then ~visiting order; unique because visiting orders are).  Level by
+// level, a histogram of the next 12 key bits of the records that share the
+// prefix chosen so far, and one warp that picks the digit where the
+// remaining count is reached; it stops as soon as the records of that digit
+// are exactly the ones still needed.  Accepted records are those whose key
+// prefix is at most the final prefix.
+// ---------------------------------------------------------------------------
+
+constexpr int kSelectBits = 12;
+constexpr int kSelectBins = 1 << kSelectBits;
+
+// `cnt` key bits starting `from` bits below the most significant bit of (k0, k1).
+__device__ __forceinline__ uint32_t key_bits(uint64_t k0, uint64_t k1, int from, int cnt) {
+    const uint64_t mask = (1ull << cnt) - 1ull;
+    if (from + cnt <= 64) return (uint32_t)((k0 >> (64 - from - cnt)) & mask);
+    if (from >= 64) return (uint32_t)((k1 >> (128 - from - cnt)) & mask);
+    const int lo = from + cnt - 64;  // bits taken from k1
+    return (uint32_t)((((k0 << lo) | (k1 >> (64 - lo)))) & mask);
+}
+
+// -1, 0, 1 as the top `bits` bits of (k0, k1) are below, equal to or above those of (p0, p1).
+__device__ __forceinline__ int prefix_cmp(uint64_t k0, uint64_t k1, uint64_t p0, uint64_t p1, int bits) {
+    if (bits <= 0) return 0;
+    if (bits <= 64) {
+        const uint64_t a = k0 >> (64 - bits), b = p0 >> (64 - bits);
+        return a < b ? -1 : (a > b ? 1 : 0);
+    }
+    if (k0 != p0) return k0 < p0 ? -1 : 1;
+    const uint64_t a = k1 >> (128 - bits), b = p1 >> (128 - bits);
+    return a < b ? -1 : (a > b ? 1 : 0);
+}
+
+__global__ void select_init_kernel(FindCtl* __restrict__ ctl, long long k, long long n,
+                                   unsigned int* __restrict__ bins) {
+    const long long valid = n - (long long)ctl->n_zero;
+    const long long need = k < valid ? k : valid;
+    for (int b = threadIdx.x; b < kSelectBins; b += blockDim.x) bins[b] = 0;
+    if (threadIdx.x == 0) {
+        ctl->sel_p0 = ctl->sel_p1 = 0;
+        ctl->sel_bits = 0;
+        ctl->sel_need = need;
+        ctl->sel_done = need <= 0 ? 1 : 0;
+        ctl->n_sel = 0;
+    }
+}
+
+__global__ void select_hist_kernel(const uint64_t* __restrict__ rank, int64_t n, int key_bits_total,
+                                   const FindCtl* __restrict__ ctl, unsigned int* __restrict__ bins) {
+    __shared__ unsigned int sh[kSelectBins];
+    if (ctl->sel_done) return;
+    const uint64_t p0 = ctl->sel_p0, p1 = ctl->sel_p1;
+    const int fixed = ctl->sel_bits;
+    const int cnt = key_bits_total - fixed < kSelectBits ? key_bits_total - fixed : kSelectBits;
+    for (int b = threadIdx.x; b < kSelectBins; b += blockDim.x) sh[b] = 0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k0 = rank[2 * i], k1 = rank[2 * i + 1];
+        if (prefix_cmp(k0, k1, p0, p1, fixed) != 0) continue;
+        atomicAdd(&sh[key_bits(k0, k1, fixed, cnt)], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kSelectBins; b += blockDim.x) {
+        const unsigned int v = sh[b];
+        if (v) atomicAdd(bins + b, v);
+    }
+}
+
+// One warp: the digit where the remaining count is reached; clears the bins.
+__global__ void select_choose_kernel(int key_bits_total, FindCtl* __restrict__ ctl, unsigned int* __restrict__ bins) {
+    const int lane = threadIdx.x;
+    if (ctl->sel_done) return;
+    const int fixed = ctl->sel_bits;
+    const int cnt = key_bits_total - fixed < kSelectBits ? key_bits_total - fixed : kSelectBits;
+    const int nbins = 1 << cnt;
+    const int per = (nbins + 31) / 32;
+    const int lo = lane * per;
+    long long mine = 0;
+    for (int b = lo; b < lo + per && b < nbins; ++b) mine += bins[b];
+    long long run = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, run, d);
+        if (lane >= d) run += y;
+    }
+    const long long need = ctl->sel_need;
+    const unsigned crossed = __ballot_sync(0xffffffffu, run >= need);
+    // crossed is never empty: the records under the prefix hold at least `need`
+    const int first = crossed ? __ffs(crossed) - 1 : 31;
+    int digit = 0;
+    long long below = 0, at = 0;
+    if (lane == first) {
+        long long acc = run - mine;
+        digit = lo + per - 1 < nbins - 1 ? lo + per - 1 : nbins - 1;
+        for (int b = lo; b < lo + per && b < nbins; ++b) {
+            if (acc + (long long)bins[b] >= need) {
+                digit = b;
+                break;
+            }
+            acc += bins[b];
+        }
+        below = acc;
+        at = bins[digit];
+    }
+    digit = __shfl_sync(0xffffffffu, digit, first);
+    below = __shfl_sync(0xffffffffu, below, first);
+    at = __shfl_sync(0xffffffffu, at, first);
+    __syncwarp();
+    for (int b = lane; b < kSelectBins; b += 32) bins[b] = 0;
+    if (lane == 0) {
+        // place the digit below the fixed bits
+        const int from = fixed;
+        uint64_t p0 = ctl->sel_p0, p1 = ctl->sel_p1;
+        const uint64_t d = (uint64_t)digit;
+        if (from + cnt <= 64) {
+            p0 |= d << (64 - from - cnt);
+        } else if (from >= 64) {
+            p1 |= d << (128 - from - cnt);
+        } else {
+            const int lo_bits = from + cnt - 64;
+            p0 |= d >> lo_bits;
+            p1 |= d << (64 - lo_bits);
+        }
+        ctl->sel_p0 = p0;
+        ctl->sel_p1 = p1;
+        ctl->sel_bits = fixed + cnt;
+        ctl->sel_need = need - below;
+        if (at == need - below || fixed + cnt >= key_bits_total) ctl->sel_done = 1;
+    }
+}
+
+// Keys of the accepted records (rank prefix at most the chosen prefix), in no particular order.
+template <int W>
+__global__ void select_compact_kernel(const uint64_t* __restrict__ rank, const uint64_t* __restrict__ keys, int64_t n,
+                                      FindCtl* __restrict__ ctl, uint64_t* __restrict__ out) {
+    const uint64_t p0 = ctl->sel_p0, p1 = ctl->sel_p1;
+    const int bits = ctl->sel_bits;
+    const bool none = ctl->sel_need <= 0 && bits == 0;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = false;
+    if (i < n && !none) take = prefix_cmp(rank[2 * i], rank[2 * i + 1], p0, p1, bits) <= 0;
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(&ctl->n_sel, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (take) {
+        const unsigned long long at = base + __popc(m & ((1u << lane) - 1u));
+#pragma unroll
+        for (int q = 0; q < W; ++q) out[at * W + q] = keys[i * W + q];
+    }
 }
 
 __global__ void zero_u64_kernel(unsigned long long* p, int n) {
@@ -257,8 +489,9 @@ struct FindArgs {
     int64_t* n_out;
 };
 
-// Workspace layout: fixed part (exclude set, packed rows, histogram, flags,
-// final row set of up to k rows), then the emission area of cap records.
+// Workspace layout: fixed part (exclude set, packed rows, histogram, control
+// block, the selected rows and their sort), then the emission area of cap
+// records.
 template <int W>
 struct FindLayout {
     HashRows excl;
@@ -266,17 +499,13 @@ struct FindLayout {
     uint64_t* keys_s;       // every kSampleStride-th row of keys_i
     double2* psi_s;         // and its amplitude
     unsigned long long* hist;
-    unsigned long long* n_emit;
-    unsigned long long* n_zero;  // emitted records of zero exact weight
-    int* overflow;
+    FindCtl* ctl;
+    unsigned int* bins;     // radix-select histogram
     uint64_t* sel_keys;
-    RowSet final_set;  // built from sel_keys through a second rowset (rows are keys here)
+    RowSet final_set;       // sort and de-duplication of the selected rows
     // emission area
     uint64_t* emit_rank;
     uint64_t* emit_keys;
-    int32_t* rank_order;
-    uint64_t* rank_sorted;
-    SortScratch rank_sort;
 };
 
 template <int W>
@@ -287,19 +516,15 @@ FindLayout<W> take_find(Arena& ws, int64_t n_i, int64_t k, int64_t n_ex, int64_t
     const int64_t n_s = n_i / kSampleStride + 1;
     L.keys_s = ws.take<uint64_t>((uint64_t)n_s * W);
     L.psi_s = ws.take<double2>((uint64_t)n_s);
-    L.hist = ws.take<unsigned long long>(kBuckets + 1);
-    L.n_emit = L.hist + kBuckets;
-    L.n_zero = ws.take<unsigned long long>(1);
-    L.overflow = ws.take<int>(1);
+    L.hist = ws.take<unsigned long long>(kBuckets);
+    L.ctl = ws.take<FindCtl>(1);
+    L.bins = ws.take<unsigned int>(kSelectBins);
     int64_t kk = k > 0 ? k : 1;
     L.sel_keys = ws.take<uint64_t>((uint64_t)kk * W);
     L.final_set = take_rowset<W>(ws, kk);
     int64_t c = cap > 0 ? cap : 1;
     L.emit_rank = ws.take<uint64_t>((uint64_t)c * 2);
     L.emit_keys = ws.take<uint64_t>((uint64_t)c * W);
-    L.rank_order = ws.take<int32_t>((uint64_t)c);
-    L.rank_sorted = ws.take<uint64_t>((uint64_t)c * 2);
-    L.rank_sort = take_sort_scratch<2>(ws, c);
     return L;
 }
 
@@ -341,8 +566,8 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     int st;
     if ((st = build_hashrows<W>(a.configs_ex, nq, L.excl, s)) != QMBX_OK) return st;
     if ((st = pack_rows<W>(a.configs_i, a.n_i, nq, L.keys_i, s)) != QMBX_OK) return st;
-    QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
-    QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
+    QMBX_CUDA_TRY(cudaMemsetAsync(L.ctl, 0, sizeof(FindCtl), s));
+    QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets, kThreads), kThreads, 0, s>>>(L.hist, kBuckets));
 
     RelativeArgs r{};
     r.psi = reinterpret_cast<const double2*>(a.psi_i);
@@ -351,28 +576,19 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
-    std::vector<unsigned long long> hist(kBuckets);
-    auto read_hist = [&]() -> int {
-        QMBX_CUDA_TRY(cudaMemcpyAsync(hist.data(), L.hist, kBuckets * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-        return QMBX_OK;
-    };
+    r.ctl = L.ctl;
+    r.cap_emit = cap;
+    r.emit_rank = L.emit_rank;
+    r.emit_keys = L.emit_keys;
     auto need_bytes = [&](unsigned long long records) {
         Arena want(nullptr, 0);
         take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)records);
         return want.used;
     };
-    // records with a zero estimate sit in bucket 0 and are emitted only when
-    // fewer than k records lie above
-    auto records_from = [&](int from) {
-        unsigned long long n = 0;
-        for (int b = from; b < kBuckets; ++b) n += hist[b];
-        return n;
-    };
 
-    // pass 1: bucket counts over every row, or every kSampleStride-th row of large inputs
+    // pass 1: bucket counts over every row, or every kSampleStride-th row of
+    // large inputs; the threshold is chosen on the device (no host round trip)
     const bool sampled = a.n_i >= kSampleMinRows;
-    int emit_from;
     if (sampled) {
         const int64_t n_s = (a.n_i + kSampleStride - 1) / kSampleStride;
         QMBX_KERNEL(kGroupOther, s, sample_rows_kernel<W><<<grid_for(n_s, kThreads), kThreads, 0, s>>>(L.keys_i, r.psi, n_s, L.keys_s, L.psi_s));
@@ -382,73 +598,49 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         rs.n_i = n_s;
         if ((st = launch_relative<W, false>(rs, L.keys_s, n_s, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
-        if ((st = read_hist()) != QMBX_OK) return st;
         // aim at about twice k records above the chosen bucket, one more bucket of slack
-        const int b_est = bucket_above(hist, (double)a.n_i / (double)n_s, 2.0 * (double)k);
-        emit_from = b_est > 1 ? b_est - 1 : 0;
-        const double est = (double)a.n_i / (double)n_s * (double)records_from(emit_from);
-        if (est > (double)cap) {
-            if (needed) *needed = need_bytes((unsigned long long)(1.5 * est) + 1);
-            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for about %.0f records near the threshold",
-                        (unsigned long long)need_bytes((unsigned long long)(1.5 * est) + 1), est);
-        }
-        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
+        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, 32, 0, s>>>(L.hist, (double)a.n_i / (double)n_s, 2.0 * (double)k, L.ctl));
     } else {
         if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
-        if ((st = read_hist()) != QMBX_OK) return st;
-        const int b_k = bucket_above(hist, 1.0, (double)k);
-        emit_from = b_k > 1 ? b_k - 1 : 0;
-        const unsigned long long need = records_from(emit_from);
-        if ((int64_t)need > cap) {
-            if (needed) *needed = need_bytes(need);
-            return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
-                        (unsigned long long)need_bytes(need), need);
-        }
-        if (need == 0) return QMBX_OK;
-        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
+        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, 32, 0, s>>>(L.hist, 1.0, (double)k, L.ctl));
     }
+    QMBX_LAUNCH_CHECK("choose_emit_kernel");
 
-    // pass 2: emit the records at or above emit_from; count every record per bucket
-    r.n_emit = L.n_emit;
-    r.cap_emit = cap;
-    r.emit_rank = L.emit_rank;
-    r.emit_keys = L.emit_keys;
-    r.overflow = L.overflow;
-    unsigned long long n_emit = 0;
+    // pass 2: emit the records at or above emit_from; count every record per
+    // bucket; the exact threshold from those counts confirms the choice
+    FindCtl ctl{};
     for (int attempt = 0;; ++attempt) {
-        r.emit_from = emit_from;
         if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
-        int overflow = 0;
-        QMBX_CUDA_TRY(cudaMemcpyAsync(&n_emit, L.n_emit, sizeof(n_emit), cudaMemcpyDeviceToHost, s));
-        QMBX_CUDA_TRY(cudaMemcpyAsync(&overflow, L.overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
-        if ((st = read_hist()) != QMBX_OK) return st;
-        // the exact threshold from pass 2's full counts
-        const int b_k = bucket_above(hist, 1.0, (double)k);
-        const int exact_from = b_k > 1 ? b_k - 1 : 0;
-        const unsigned long long need = records_from(exact_from < emit_from ? exact_from : emit_from);
-        if (overflow || (int64_t)n_emit > cap) {
-            if (needed) *needed = need_bytes(need);
+        QMBX_KERNEL(kGroupSelect, s, check_emit_kernel<<<1, 32, 0, s>>>(L.hist, (double)k, L.ctl));
+        QMBX_LAUNCH_CHECK("check_emit_kernel");
+        QMBX_CUDA_TRY(cudaMemcpyAsync(&ctl, L.ctl, sizeof(FindCtl), cudaMemcpyDeviceToHost, s));
+        QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+        if (ctl.overflow || (int64_t)ctl.n_emit > cap) {
+            if (needed) *needed = need_bytes(ctl.need > ctl.n_emit ? ctl.need : ctl.n_emit);
             return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
-                        (unsigned long long)need_bytes(need), need);
+                        (unsigned long long)need_bytes(ctl.need), ctl.need);
         }
-        if (emit_from <= exact_from) break;  // every record down to the k-th was kept
+        if (ctl.emit_from <= ctl.exact_from) break;  // every record down to the k-th was kept
         if (attempt > 0) return fail(QMBX_ERR_DEVICE, "find_relative threshold did not settle");
         // the sampled counts put the threshold too high: again with the exact one
-        emit_from = exact_from;
-        if ((int64_t)records_from(emit_from) > cap) {
-            if (needed) *needed = need_bytes(records_from(emit_from));
+        if ((int64_t)ctl.need > cap) {
+            if (needed) *needed = need_bytes(ctl.need);
             return fail(QMBX_ERR_WORKSPACE, "find_relative needs %llu bytes of workspace for %llu records near the threshold",
-                        (unsigned long long)need_bytes(records_from(emit_from)), records_from(emit_from));
+                        (unsigned long long)need_bytes(ctl.need), ctl.need);
         }
-        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets + 1, kThreads), kThreads, 0, s>>>(L.hist, kBuckets + 1));
-        QMBX_CUDA_TRY(cudaMemsetAsync(L.overflow, 0, sizeof(int), s));
+        FindCtl reset = ctl;
+        reset.n_emit = 0;
+        reset.overflow = 0;
+        reset.emit_from = ctl.exact_from;
+        QMBX_CUDA_TRY(cudaMemcpyAsync(L.ctl, &reset, sizeof(FindCtl), cudaMemcpyHostToDevice, s));
+        QMBX_KERNEL(kGroupOther, s, zero_u64_kernel<<<grid_for(kBuckets, kThreads), kThreads, 0, s>>>(L.hist, kBuckets));
+        QMBX_CUDA_TRY(cudaStreamSynchronize(s));  // `reset` lives on this frame
     }
-    g_find_stats.records = (int64_t)n_emit;
-    if (n_emit == 0) return QMBX_OK;
-    const int64_t e = (int64_t)n_emit;
-    QMBX_CUDA_TRY(cudaMemsetAsync(L.n_zero, 0, sizeof(unsigned long long), s));
+    g_find_stats.records = (int64_t)ctl.n_emit;
+    if (ctl.n_emit == 0) return QMBX_OK;
+    const int64_t e = (int64_t)ctl.n_emit;
     // bytes of the visiting order (term index * n_i + row < n_terms * n_i)
     int order_bytes = 1;
     {
@@ -456,34 +648,35 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         while (order_bytes < 8 && span > std::ldexp(1.0, 8 * order_bytes)) ++order_bytes;
     }
     const int order_shift = 64 - 8 * order_bytes;
-    QMBX_KERNEL(kGroupSelect, s, rank_records_kernel<<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, e, r.off, r.diag, r.psi, a.n_i, order_shift, L.n_zero));
+    const int key_bits_total = 64 + 8 * order_bytes;
+    QMBX_KERNEL(kGroupSelect, s, rank_records_kernel<<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, e, r.off, r.diag, r.psi, a.n_i, order_shift, &L.ctl->n_zero));
     QMBX_LAUNCH_CHECK("rank_records_kernel");
-    if ((st = sort_pairs<2>(L.emit_rank, nullptr, L.rank_sorted, L.rank_order, e, 8 + order_bytes, L.rank_sort, s)) != QMBX_OK) {
-        return st;
+    // radix select of the k smallest rank keys (zero-weight records rank last and are never taken)
+    QMBX_KERNEL(kGroupSelect, s, select_init_kernel<<<1, 256, 0, s>>>(L.ctl, (long long)k, (long long)e, L.bins));
+    const int levels = (key_bits_total + kSelectBits - 1) / kSelectBits;
+    const unsigned sel_grid = grid_for(e, kThreads) < 2u * 152u ? grid_for(e, kThreads) : 2u * 152u;
+    for (int level = 0; level < levels; ++level) {
+        QMBX_KERNEL(kGroupSelect, s, select_hist_kernel<<<sel_grid, kThreads, 0, s>>>(L.emit_rank, e, key_bits_total, L.ctl, L.bins));
+        QMBX_KERNEL(kGroupSelect, s, select_choose_kernel<<<1, 32, 0, s>>>(key_bits_total, L.ctl, L.bins));
     }
-    unsigned long long n_zero = 0;
-    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_zero, L.n_zero, sizeof(n_zero), cudaMemcpyDeviceToHost, s));
+    QMBX_KERNEL(kGroupSelect, s, select_compact_kernel<W><<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, L.emit_keys, e, L.ctl, L.sel_keys));
+    QMBX_LAUNCH_CHECK("find_relative selection");
+    unsigned long long n_sel = 0;
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&n_sel, &L.ctl->n_sel, sizeof(n_sel), cudaMemcpyDeviceToHost, s));
     QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-    // zero-weight records sort last and are never selected
-    const int64_t valid = e - (int64_t)n_zero;
-    if (valid <= 0) return QMBX_OK;
-    const int64_t keep = valid < k ? valid : k;
-    // rank keys of 16 bytes + 4-byte record index per item; selected rows of 8W bytes + 4-byte index
+    const int64_t keep = (int64_t)n_sel;
+    if (keep == 0) return QMBX_OK;
+    if (keep > k) return fail(QMBX_ERR_DEVICE, "find_relative selected %lld records for %lld places", (long long)keep, (long long)k);
+    // sort and de-duplicate the selected rows, then unpack the distinct ones
     g_find_stats.selected = keep;
-    g_find_stats.sort_passes = (8 + order_bytes) + nq;
-    g_find_stats.sort_bytes = (int64_t)(8 + order_bytes) * 2 * e * (16 + 4) + (int64_t)nq * 2 * keep * (8 * W + 4);
-    QMBX_KERNEL(kGroupSelect, s, gather_selected_kernel<W><<<grid_for(keep, kThreads), kThreads, 0, s>>>(L.rank_order, L.emit_keys, keep,
-                                                                            L.sel_keys));
-    QMBX_LAUNCH_CHECK("gather_selected_kernel");
-    // sort and de-duplicate the selected rows: unpack to bytes in the output
-    // buffer, then build a row set from those bytes
-    if ((st = unpack_rows<W>(L.sel_keys, nullptr, keep, nq, a.out, s)) != QMBX_OK) return st;
+    g_find_stats.sort_passes = nq;
+    // per pass: the selected keys (8W bytes) and their 4-byte index, read and written
+    g_find_stats.sort_bytes = (int64_t)nq * 2 * keep * (8 * W + 4);
     L.final_set.n = keep;
-    if ((st = build_rowset<W>(a.out, nq, L.final_set, s)) != QMBX_OK) return st;
+    if ((st = sort_unique_keys<W>(L.sel_keys, nq, L.final_set, s)) != QMBX_OK) return st;
+    if ((st = unpack_rows<W>(L.final_set.keys, L.final_set.count, keep, nq, a.out, s)) != QMBX_OK) return st;
     int n_unique = 0;
     QMBX_CUDA_TRY(cudaMemcpyAsync(&n_unique, L.final_set.count, sizeof(int), cudaMemcpyDeviceToHost, s));
-    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-    if ((st = unpack_rows<W>(L.final_set.keys, nullptr, n_unique, nq, a.out, s)) != QMBX_OK) return st;
     QMBX_CUDA_TRY(cudaStreamSynchronize(s));
     *a.n_out = n_unique;
     g_find_stats.rows_out = n_unique;

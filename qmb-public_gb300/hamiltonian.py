@@ -81,6 +81,11 @@ class _Table:
             self._hermitian = bool(flag.value)
         return self._hermitian
 
+    def use_on(self, stream: torch.cuda.Stream) -> None:
+        """Mark the device blob as used by work on `stream`, so that torch's caching allocator does not
+        hand its memory out again (after the table is dropped) before that work has finished."""
+        self.dev.record_stream(stream)
+
     @property
     def h(self) -> int:
         return self.host.data_ptr()
@@ -133,6 +138,8 @@ class Hamiltonian:
             # versions of them) are stale; those for other row widths are kept
             self._tables = {k: v for k, v in self._tables.items() if k[0] != device.index or k[2:] == key[2:]}
             self._tables[key] = table
+        # every caller launches work that reads the table on the current stream
+        table.use_on(torch.cuda.current_stream(device))
         return table
 
     @staticmethod

@@ -35,22 +35,22 @@ def _abs_scale(g, configs_i, psi_i, configs_j):
                                       configs_j, 2))
 
 
-def _with_workspace(table, ci, psi, cj, device):
+def _with_workspace(table, ci, psi, cj, device, same=0):
     lib = _native.library()
     need = ctypes.c_uint64()
     _native.check(lib.qmbx_apply_within_workspace(table.h, ci.shape[0], cj.shape[0], ctypes.byref(need)))
     ws = torch.empty(max(need.value, 256), dtype=torch.uint8, device=device)
     out = torch.empty(cj.shape[0], dtype=torch.complex128, device=device)
     _native.check(lib.qmbx_apply_within(table.h, table.d, ci.data_ptr(), psi.data_ptr(), ci.shape[0], cj.data_ptr(),
-                                        cj.shape[0], 0, out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                        cj.shape[0], same, out.data_ptr(), ws.data_ptr(), ws.numel(),
                                         torch.cuda.current_stream(device).cuda_stream))
     return out
 
 
-def _static(table, ci, psi, cj, device):
+def _static(table, ci, psi, cj, device, same=0):
     out = torch.empty(cj.shape[0], dtype=torch.complex128, device=device)
     _native.check(_native.library().qmbx_apply_within_static(table.h, table.d, ci.data_ptr(), psi.data_ptr(),
-                                                             ci.shape[0], cj.data_ptr(), cj.shape[0], 0,
+                                                             ci.shape[0], cj.data_ptr(), cj.shape[0], same,
                                                              out.data_ptr(),
                                                              torch.cuda.current_stream(device).cuda_stream))
     return out
@@ -104,3 +104,29 @@ def test_static_scratch_refuses_oversized_inputs(cuda_device):
         got = _static(table, small, p, small, cuda_device).cpu().numpy()
         want = _with_workspace(table, small, p, small, cuda_device).cpu().numpy()
         assert np.allclose(got, want, rtol=0, atol=1e-12 * (1 + np.abs(want).max()))
+
+
+def test_static_scratch_same_configs_after_a_larger_call(cuda_device):
+    # same_configs = 1 builds one row set in the shared scratch; run it right
+    # after a larger call (two sets of 20,000 random rows) so that anything
+    # that call left behind would show
+    g = golden("random_terms_fermi")
+    ham = Hamiltonian((torch.from_numpy(g["site"]), torch.from_numpy(g["kind"]), torch.from_numpy(g["coef"])),
+                      kind="fermi")
+    nq = g["configs_i"].shape[1]
+    rng = np.random.default_rng(5)
+    with torch.cuda.device(cuda_device):
+        table = ham._table(cuda_device, nq)
+        big_i = torch.from_numpy(rng.integers(0, 256, size=(20000, nq), dtype=np.uint8)).to(cuda_device)
+        big_j = torch.from_numpy(rng.integers(0, 256, size=(20000, nq), dtype=np.uint8)).to(cuda_device)
+        big_psi = torch.randn(20000, dtype=torch.complex128, device=cuda_device)
+        _static(table, big_i, big_psi, big_j, cuda_device)
+        rows = np.unique(np.concatenate([g["configs_i"], g["configs_j"]]), axis=0)
+        psi_np = rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])
+        r = torch.from_numpy(rows).to(cuda_device)
+        psi = torch.from_numpy(psi_np).to(cuda_device)
+        got = _static(table, r, psi, r, cuda_device, same=1).cpu().numpy()
+        want = _with_workspace(table, r, psi, r, cuda_device, same=1).cpu().numpy()
+        scale = _abs_scale(g, rows, psi_np, rows)
+        assert np.count_nonzero(want) > 100
+        assert np.all(np.abs(got - want) <= RTOL_F64 * scale + 1e-300)
