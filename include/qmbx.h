@@ -69,6 +69,10 @@ int qmbx_table_bytes(const int16_t* site, const uint8_t* kind, int64_t n_terms, 
 int qmbx_table_build(const int16_t* site, const uint8_t* kind, const double* coef, int64_t n_terms, int32_t n_qubytes,
                      int32_t particle_cut, void* blob, uint64_t blob_bytes);
 
+/* QMBX_OK when blob (blob_bytes long) holds a whole table of the format this
+ * library reads, e.g. one written to a cache file by an earlier process. */
+int qmbx_table_check(const void* blob, uint64_t blob_bytes);
+
 /* Counts read from a compiled table: [n_terms, live terms, diagonal terms, n_qubytes, particle_cut, n_words]. */
 int qmbx_table_counts(const void* table_host, int64_t counts[6]);
 
@@ -154,6 +158,32 @@ int qmbx_apply_within_adjoint_f32c(const void* table_host, const void* table_dev
                                    void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * H restricted to one set of n distinct rows as a sparse matrix (no
+ * counterpart in the reference, whose Lanczos loops, qmb/rldiag.py:19-52 and
+ * qmb/haar.py:107-183, call apply_within on the same rows every iteration).
+ * CSR layout: row j holds entries [row_ptr[j], row_ptr[j + 1]): first the
+ * diagonal (column j, possibly zero), then one entry (column i, value = the
+ * term's signed coefficient) per (term, row i) mapping row i onto row j.
+ * qmbx_matrix_count writes row_ptr (n + 1 device int64) and stores the entry
+ * count in *nnz (host); it synchronises the stream.  qmbx_matrix_fill then
+ * writes col (nnz int32) and val (nnz complex128) for the same rows and
+ * table.  qmbx_matrix_apply computes y = A x (complex128) with a fixed
+ * summation order.  Limits: distinct rows, nnz below 2^31.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_matrix_workspace(const void* table_host, int64_t n, uint64_t* bytes);
+
+int qmbx_matrix_count(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n,
+                      int64_t* row_ptr, int64_t* nnz, void* workspace, uint64_t workspace_bytes, qmbx_stream_t stream);
+
+int qmbx_matrix_fill(const void* table_host, const void* table_dev, const uint8_t* configs, int64_t n,
+                     const int64_t* row_ptr, int32_t* col, double* val, void* workspace, uint64_t workspace_bytes,
+                     qmbx_stream_t stream);
+
+int qmbx_matrix_apply(int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val, const double* x,
+                      double* y, qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * diagonal_term: out[c] = sum of s * coef_t over terms with t|c> = s|c>.
  * Replaces diagonal_term_interface (qmb/_hamiltonian_cuda.cu:710-803).
  * Needs no workspace.
@@ -193,6 +223,26 @@ int qmbx_find_relative(const void* table_host, const void* table_dev, const uint
  * selected rows, [3] bytes those passes move (passes x 2 x items x item
  * bytes), [4] records selected before de-duplication, [5] rows returned. */
 int qmbx_find_relative_stats(int64_t stats[6]);
+
+/* ---------------------------------------------------------------------------
+ * The Epstein-Nesbet PT2 step of qmb/pert.py:37-61 in one call (the
+ * reference composes it in Python from apply_within, find_relative,
+ * apply_within and diagonal_term):
+ *   energies[0] = E0 = Re<psi|H|psi> / <psi|psi> over configs (n distinct rows),
+ *   other = find_relative(configs, psi, count_selected, configs),
+ *   energies[1] = E2 = sum over other of |(H psi)_j|^2 / <psi|psi> / (E0 - Re H_jj),
+ * *n_other = the number of rows of other.  E0 is summed by find_relative's
+ * emission pass (its exclusion set is configs), so the step walks the terms
+ * once fewer than the composition.  count_selected >= 1.  Synchronises the
+ * stream.  Workspace as for qmbx_find_relative: on QMBX_ERR_WORKSPACE
+ * *workspace_needed holds the size to retry with.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_pt2_workspace(const void* table_host, int64_t n, int64_t count_selected, uint64_t* bytes);
+
+int qmbx_pt2(const void* table_host, const void* table_dev, const uint8_t* configs, const double* psi, int64_t n,
+             int64_t count_selected, double* energies, int64_t* n_other, void* workspace, uint64_t workspace_bytes,
+             uint64_t* workspace_needed, qmbx_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * single_relative: for every row, one image outside the row set drawn with

@@ -7,7 +7,7 @@ in hand-written sm_103a CUDA kernels behind the C ABI of include/qmbx.h.
 
 from . import bitspack, terms  # noqa: F401
 from .energy import variational_energy  # noqa: F401
-from .hamiltonian import Hamiltonian  # noqa: F401
+from .hamiltonian import Hamiltonian, HamiltonianMatrix  # noqa: F401
 from .solvers import lanczos_energy, pt2_energy  # noqa: F401
 
-__all__ = ["Hamiltonian", "variational_energy", "lanczos_energy", "pt2_energy", "bitspack", "terms"]
+__all__ = ["Hamiltonian", "HamiltonianMatrix", "variational_energy", "lanczos_energy", "pt2_energy", "bitspack", "terms"]

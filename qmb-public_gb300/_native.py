@@ -35,6 +35,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_table_bytes": (ctypes.c_int, [_P, _P, _I64, _I32, _I32, _PU64]),
     "qmbx_table_build": (ctypes.c_int, [_P, _P, _P, _I64, _I32, _I32, _P, _U64]),
     "qmbx_table_counts": (ctypes.c_int, [_P, _PI64]),
+    "qmbx_table_check": (ctypes.c_int, [_P, _U64]),
     "qmbx_table_hermitian": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     "qmbx_apply_within_workspace": (ctypes.c_int, [_P, _I64, _I64, _PU64]),
     "qmbx_apply_within": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P, _U64, _P]),
@@ -43,9 +44,15 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_apply_within_f32c": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
     "qmbx_apply_within_adjoint_f32c": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
     "qmbx_diagonal_term": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P]),
+    "qmbx_matrix_workspace": (ctypes.c_int, [_P, _I64, _PU64]),
+    "qmbx_matrix_count": (ctypes.c_int, [_P, _P, _P, _I64, _P, _PI64, _P, _U64, _P]),
+    "qmbx_matrix_fill": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P, _U64, _P]),
+    "qmbx_matrix_apply": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P]),
     "qmbx_find_relative_workspace": (ctypes.c_int, [_P, _I64, _I64, _I64, _PU64]),
     "qmbx_find_relative": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _I64, _P, _PI64, _P, _U64, _PU64, _P]),
     "qmbx_find_relative_stats": (ctypes.c_int, [_PI64]),
+    "qmbx_pt2_workspace": (ctypes.c_int, [_P, _I64, _I64, _PU64]),
+    "qmbx_pt2": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _PI64, _P, _U64, _PU64, _P]),
     "qmbx_single_relative_workspace": (ctypes.c_int, [_P, _I64, _PU64]),
     "qmbx_single_relative": (ctypes.c_int, [_P, _P, _P, _I64, _U64, _P, _P, _U64, _P]),
     "qmbx_profile_enable": (ctypes.c_int, [_I32]),

@@ -99,6 +99,13 @@ struct RelativeArgs {
     uint64_t* emit_rank;     // [cap][2]: (slot | part << 62 | parity << 63, row) from the walk;
                              // (~weight bits, ~order) after rank_records_kernel
     uint64_t* emit_keys;     // [cap][W]
+    // when non-NULL (the PT2 step, whose exclusion set is configs_i itself):
+    // the emission pass also sums conj(psi_ex[j]) * s * coef * psi[i] over
+    // the records whose image j IS excluded, i.e. the numerator of
+    // <psi|H|psi>, into e0[blockIdx.x % e0_slots]
+    double2* e0;
+    const double2* psi_ex;
+    int e0_slots;
 };
 
 template <int W, bool EMIT>
@@ -110,6 +117,7 @@ struct RelativeVisitor : VisitorBase {
         float m;
         int64_t row;
         int* hist;
+        double e0re, e0im;
     };
     // both passes count every record per bucket (pass 2's counts confirm pass 1's choice)
     __device__ __forceinline__ void block_init(int* sh) const {
@@ -128,6 +136,27 @@ struct RelativeVisitor : VisitorBase {
         acc.m = __fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py));
         acc.row = row;
         acc.hist = sh;
+        acc.e0re = acc.e0im = 0.0;
+    }
+    // conj(psi_ex[pos]) * s * coef * psi_row, added to the <psi|H|psi> partial
+    __device__ __forceinline__ void add_e0(Acc& acc, double2 cf, int parity, int64_t pos) const {
+        const double2 q = __ldg(a.psi_ex + pos);
+        double tr = cf.x * acc.p.x - cf.y * acc.p.y;
+        double ti = cf.x * acc.p.y + cf.y * acc.p.x;
+        if (parity) {
+            tr = -tr;
+            ti = -ti;
+        }
+        acc.e0re += q.x * tr + q.y * ti;
+        acc.e0im += q.x * ti - q.y * tr;
+    }
+    __device__ __forceinline__ void flush_e0(Acc& acc) const {
+        if (acc.e0re != 0.0 || acc.e0im != 0.0) {
+            double2* slot = a.e0 + (blockIdx.x % a.e0_slots);
+            atomicAdd(&slot->x, acc.e0re);
+            atomicAdd(&slot->y, acc.e0im);
+        }
+        acc.e0re = acc.e0im = 0.0;
     }
     static constexpr bool kProbe = true;
     HashView lookup;  // the exclusion set
@@ -157,13 +186,35 @@ struct RelativeVisitor : VisitorBase {
         return false;
     }
     __device__ __forceinline__ void visit(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        if (hash_find<W>(lookup, img) < 0) record(acc, img, a.off, 0, parity, slot);
+        const int64_t pos = hash_find<W>(lookup, img);
+        if (pos < 0) {
+            record(acc, img, a.off, 0, parity, slot);
+        } else if (EMIT && a.e0 != nullptr) {
+            add_e0(acc, __ldg(a.off.coef + slot), parity, pos);
+        }
     }
     __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
-        if (hash_find<W>(lookup, c) < 0) record(acc, c, a.diag, 1, parity, slot);
+        const int64_t pos = hash_find<W>(lookup, c);
+        if (pos < 0) {
+            record(acc, c, a.diag, 1, parity, slot);
+        } else if (EMIT && a.e0 != nullptr) {
+            add_e0(acc, __ldg(a.diag.coef + slot), parity, pos);
+        }
     }
-    __device__ __forceinline__ void reduce(Acc&) const {}
-    __device__ __forceinline__ void finish(Acc&, int64_t, const Key<W>&) const {}
+    __device__ __forceinline__ void reduce(Acc& acc) const {
+        if (EMIT && a.e0 != nullptr) {
+            acc.e0re = warp_sum(acc.e0re);
+            acc.e0im = warp_sum(acc.e0im);
+        }
+    }
+    // grouped walks: lane 0 after reduce(); tiled walks: every thread
+    __device__ __forceinline__ void finish(Acc& acc, int64_t, const Key<W>&) const {
+        if (EMIT && a.e0 != nullptr) flush_e0(acc);
+    }
+    // pivot-major walks: one (row, group) partial
+    __device__ __forceinline__ void flush(Acc& acc, int64_t, const Key<W>&) const {
+        if (EMIT && a.e0 != nullptr) flush_e0(acc);
+    }
 };
 
 template <int W, bool EMIT>
@@ -487,6 +538,8 @@ struct FindArgs {
     int64_t n_ex;
     uint8_t* out;
     int64_t* n_out;
+    double2* e0;        // PT2 only (see RelativeArgs::e0); NULL otherwise
+    int e0_slots;
 };
 
 // Workspace layout: fixed part (exclude set, packed rows, histogram, control
@@ -580,6 +633,9 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.cap_emit = cap;
     r.emit_rank = L.emit_rank;
     r.emit_keys = L.emit_keys;
+    r.e0 = a.e0;
+    r.psi_ex = r.psi;
+    r.e0_slots = a.e0_slots;
     auto need_bytes = [&](unsigned long long records) {
         Arena want(nullptr, 0);
         take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)records);
@@ -611,6 +667,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     // bucket; the exact threshold from those counts confirms the choice
     FindCtl ctl{};
     for (int attempt = 0;; ++attempt) {
+        if (a.e0 != nullptr) QMBX_CUDA_TRY(cudaMemsetAsync(a.e0, 0, (size_t)a.e0_slots * sizeof(double2), s));
         if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
         QMBX_KERNEL(kGroupSelect, s, check_emit_kernel<<<1, 32, 0, s>>>(L.hist, (double)k, L.ctl));
@@ -865,7 +922,8 @@ extern "C" int qmbx_find_relative(const void* table_host, const void* table_dev,
     if (count_selected > 0 && out == nullptr) return fail(QMBX_ERR_ARGUMENT, "out must not be NULL");
     if ((st = check_ws(workspace)) != QMBX_OK) return st;
     if (workspace == nullptr) workspace_bytes = 0;
-    FindArgs a{table_host, table_dev, configs_i, psi_i, n_i, count_selected, configs_exclude, n_exclude, out, n_out};
+    FindArgs a{table_host, table_dev, configs_i, psi_i, n_i, count_selected, configs_exclude, n_exclude, out, n_out,
+               nullptr, 0};
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     switch (header_of(table_host)->n_words) {
         case 1: return find_impl<1>(a, workspace, workspace_bytes, workspace_needed, s);
@@ -926,4 +984,185 @@ extern "C" int qmbx_single_relative(const void* table_host, const void* table_de
         case 4: return single_impl<4>(table_host, table_dev, configs, n, seed, out, ws, s);
         default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
     }
+}
+
+// ---------------------------------------------------------------------------
+// The Epstein-Nesbet PT2 step of qmb/pert.py:37-61 in one call:
+//   E0 = Re<psi|H|psi> / <psi|psi> over configs,
+//   other = find_relative(configs, psi, count_selected, configs),
+//   E2 = sum_j |(H psi)_j|^2 / <psi|psi> / (E0 - Re H_jj) over other.
+// The reference walks the terms four times (apply_within for E0,
+// find_relative, apply_within onto other, diagonal_term).  Here E0 comes out
+// of find_relative's emission pass: its exclusion set is configs itself, so
+// the records it skips are exactly the terms of <psi|H|psi>; the remaining
+// walks are find_relative's sampled threshold pass, the scatter of H psi
+// onto the selected rows and the diagonal terms of those rows, all on the
+// device with E0 never leaving it.
+// ---------------------------------------------------------------------------
+
+namespace qmbx {
+namespace {
+
+constexpr int kE0Slots = 1024;
+constexpr int kPt2Blocks = 1024;
+
+// Deterministic block sum of one double per thread (blockDim.x a multiple of 32, at most 1024).
+__device__ __forceinline__ double block_sum(double x, double* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    x = warp_sum(x);
+    if (lane == 0) s_warp[warp] = x;
+    __syncthreads();
+    double t = lane < nwarps ? s_warp[lane] : 0.0;
+    if (warp == 0) t = warp_sum(t);
+    __syncthreads();
+    return t;  // valid in warp 0
+}
+
+// sums[0] = E0 = Re(sum of the slots) / norm, sums[1] = norm = <psi|psi>
+__global__ void pt2_e0_kernel(const double2* __restrict__ slots, int n_slots, const double2* __restrict__ psi,
+                              int64_t n, double* __restrict__ sums) {
+    __shared__ double s_warp[32];
+    double num = 0.0, norm = 0.0;
+    for (int k = threadIdx.x; k < n_slots; k += blockDim.x) num += slots[k].x;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 p = psi[i];
+        norm += p.x * p.x + p.y * p.y;
+    }
+    num = block_sum(num, s_warp);
+    norm = block_sum(norm, s_warp);
+    if (threadIdx.x == 0) {
+        sums[0] = num / norm;
+        sums[1] = norm;
+    }
+}
+
+// partials[b] = sum over the rows of block b of |h_j|^2 / norm / (E0 - Re d_j)
+__global__ void pt2_terms_kernel(const double2* __restrict__ hpsi, const double2* __restrict__ diag, int64_t m,
+                                 const double* __restrict__ sums, double* __restrict__ partials) {
+    __shared__ double s_warp[32];
+    const double e0 = sums[0], norm = sums[1];
+    double acc = 0.0;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = hpsi[j];
+        acc += (h.x * h.x + h.y * h.y) / norm / (e0 - diag[j].x);
+    }
+    acc = block_sum(acc, s_warp);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+__global__ void pt2_sum_kernel(const double* __restrict__ partials, int nb, double* __restrict__ sums) {
+    __shared__ double s_warp[32];
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) acc += partials[k];
+    acc = block_sum(acc, s_warp);
+    if (threadIdx.x == 0) sums[2] = acc;
+}
+
+struct Pt2Layout {
+    uint8_t* rows;
+    double2* hpsi;
+    double2* diag;
+    double2* slots;
+    double* sums;
+    double* partials;
+};
+
+Pt2Layout take_pt2(Arena& ws, int64_t k, int nq) {
+    Pt2Layout L;
+    const uint64_t kk = (uint64_t)(k > 0 ? k : 1);
+    L.rows = ws.take<uint8_t>(kk * (uint64_t)nq);
+    L.hpsi = ws.take<double2>(kk);
+    L.diag = ws.take<double2>(kk);
+    L.slots = ws.take<double2>(kE0Slots);
+    L.sums = ws.take<double>(4);
+    L.partials = ws.take<double>(kPt2Blocks);
+    return L;
+}
+
+}  // namespace
+}  // namespace qmbx
+
+extern "C" int qmbx_pt2_workspace(const void* table_host, int64_t n, int64_t count_selected, uint64_t* bytes) {
+    clear_error();
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    Arena fixed(nullptr, 0);
+    take_pt2(fixed, count_selected, h->n_qubytes);
+    uint64_t find = 0, apply = 0;
+    int st = qmbx_find_relative_workspace(table_host, n, count_selected, n, &find);
+    if (st != QMBX_OK) return st;
+    if ((st = qmbx_apply_within_workspace(table_host, n, count_selected, &apply)) != QMBX_OK) return st;
+    *bytes = fixed.used + (find > apply ? find : apply);
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_pt2(const void* table_host, const void* table_dev, const uint8_t* configs, const double* psi,
+                        int64_t n, int64_t count_selected, double* energies, int64_t* n_other, void* workspace,
+                        uint64_t workspace_bytes, uint64_t* workspace_needed, qmbx_stream_t stream) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if (energies == nullptr || n_other == nullptr) return fail(QMBX_ERR_ARGUMENT, "energies and n_other must not be NULL");
+    if (n <= 0 || n >= (int64_t(1) << 31)) return fail(QMBX_ERR_ARGUMENT, "row count out of range");
+    if (configs == nullptr || psi == nullptr) return fail(QMBX_ERR_ARGUMENT, "input pointers must not be NULL");
+    if (count_selected <= 0 || count_selected >= (int64_t(1) << 31)) {
+        return fail(QMBX_ERR_ARGUMENT, "count_selected must be positive and below 2^31");
+    }
+    if ((st = check_ws(workspace)) != QMBX_OK) return st;
+    const qmbx_table_header* h = header_of(table_host);
+    Arena fixed(workspace, workspace == nullptr ? 0 : workspace_bytes);
+    Pt2Layout L = take_pt2(fixed, count_selected, h->n_qubytes);
+    if (workspace == nullptr || !fixed.fits()) {
+        uint64_t want = 0;
+        qmbx_pt2_workspace(table_host, n, count_selected, &want);
+        if (workspace_needed) *workspace_needed = want;
+        return fail(QMBX_ERR_WORKSPACE, "pt2 needs at least %llu bytes of workspace", (unsigned long long)want);
+    }
+    void* scratch = static_cast<char*>(workspace) + fixed.used;
+    const uint64_t scratch_bytes = workspace_bytes - fixed.used;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    *n_other = 0;
+    // find_relative with the E0 numerator summed by its emission pass
+    FindArgs a{table_host, table_dev, configs, psi, n, count_selected, configs, n, L.rows, n_other, L.slots, kE0Slots};
+    uint64_t find_needed = 0;
+    switch (h->n_words) {
+        case 1: st = find_impl<1>(a, scratch, scratch_bytes, &find_needed, s); break;
+        case 2: st = find_impl<2>(a, scratch, scratch_bytes, &find_needed, s); break;
+        case 3: st = find_impl<3>(a, scratch, scratch_bytes, &find_needed, s); break;
+        case 4: st = find_impl<4>(a, scratch, scratch_bytes, &find_needed, s); break;
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
+    if (st == QMBX_ERR_WORKSPACE && workspace_needed) *workspace_needed = fixed.used + find_needed;
+    if (st != QMBX_OK) return st;
+    const int64_t m = *n_other;
+    QMBX_KERNEL(kGroupSelect, s, pt2_e0_kernel<<<1, 1024, 0, s>>>(L.slots, kE0Slots, reinterpret_cast<const double2*>(psi), n, L.sums));
+    QMBX_LAUNCH_CHECK("pt2_e0_kernel");
+    if (m > 0) {
+        // H psi onto the selected rows, and their diagonal terms
+        if ((st = qmbx_apply_within(table_host, table_dev, configs, psi, n, L.rows, m, 0,
+                                    reinterpret_cast<double*>(L.hpsi), scratch, scratch_bytes, stream)) != QMBX_OK) {
+            if (st == QMBX_ERR_WORKSPACE && workspace_needed) {
+                uint64_t apply = 0;
+                qmbx_apply_within_workspace(table_host, n, m, &apply);
+                *workspace_needed = fixed.used + apply;
+            }
+            return st;
+        }
+        if ((st = qmbx_diagonal_term(table_host, table_dev, L.rows, m, reinterpret_cast<double*>(L.diag), stream)) != QMBX_OK) {
+            return st;
+        }
+        const unsigned nb = grid_for(m, 256) < (unsigned)kPt2Blocks ? grid_for(m, 256) : (unsigned)kPt2Blocks;
+        QMBX_KERNEL(kGroupSelect, s, pt2_terms_kernel<<<nb, 256, 0, s>>>(L.hpsi, L.diag, m, L.sums, L.partials));
+        QMBX_KERNEL(kGroupSelect, s, pt2_sum_kernel<<<1, 1024, 0, s>>>(L.partials, (int)nb, L.sums));
+        QMBX_LAUNCH_CHECK("pt2 sums");
+    } else {
+        QMBX_CUDA_TRY(cudaMemsetAsync(L.sums + 2, 0, sizeof(double), s));
+    }
+    double out[3] = {0.0, 0.0, 0.0};
+    QMBX_CUDA_TRY(cudaMemcpyAsync(out, L.sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    energies[0] = out[0];
+    energies[1] = out[2];
+    return QMBX_OK;
 }

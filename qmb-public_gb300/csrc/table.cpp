@@ -370,6 +370,21 @@ extern "C" int qmbx_table_build(const int16_t* site, const uint8_t* kind, const 
     return QMBX_OK;
 }
 
+extern "C" int qmbx_table_check(const void* blob, uint64_t blob_bytes) {
+    clear_error();
+    const qmbx_table_header* h = static_cast<const qmbx_table_header*>(blob);
+    if (h == nullptr || blob_bytes < sizeof(qmbx_table_header)) return fail(QMBX_ERR_ARGUMENT, "blob too short for a table");
+    if (h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    if (h->version != QMBX_TABLE_VERSION) {
+        return fail(QMBX_ERR_ARGUMENT, "table format %u, this library reads %u", h->version, QMBX_TABLE_VERSION);
+    }
+    if (h->total_bytes != blob_bytes) {
+        return fail(QMBX_ERR_ARGUMENT, "table of %llu bytes in a blob of %llu", (unsigned long long)h->total_bytes,
+                    (unsigned long long)blob_bytes);
+    }
+    return QMBX_OK;
+}
+
 extern "C" int qmbx_table_counts(const void* table_host, int64_t counts[6]) {
     clear_error();
     const qmbx_table_header* h = static_cast<const qmbx_table_header*>(table_host);

@@ -15,12 +15,18 @@ CUDA kernels of libqmbx.so on the configurations' device through the C ABI
 Additions over the reference: complex64 amplitudes select the FP32 path with
 compensated accumulation; ``apply_within`` is differentiable in ``psi_i``
 (its backward is the adjoint kernel); ``apply_within_adjoint`` exposes that
-kernel directly.
+kernel directly; ``matrix`` materialises H on a fixed basis (for iterative
+eigensolvers); ``pt2`` runs the Epstein-Nesbet step of qmb/pert.py in one
+call; ``table_cache=`` (or QMBX_TABLE_CACHE) caches compiled term tables on
+disk.
 """
 
 from __future__ import annotations
 
 import ctypes
+import hashlib
+import os
+import struct
 
 import numpy as np
 import torch
@@ -28,7 +34,7 @@ import torch
 from . import _native
 from .terms import prepare, sort_terms
 
-__all__ = ["Hamiltonian"]
+__all__ = ["Hamiltonian", "HamiltonianMatrix"]
 
 
 def _ptr(t: torch.Tensor | None) -> int | None:
@@ -46,24 +52,64 @@ def _workspace(nbytes: int, device: torch.device) -> torch.Tensor:
     return ws
 
 
+def _pinned(nbytes: int) -> torch.Tensor:
+    """A host buffer for a table blob: page-locked where a GPU is present, so the device copy is one DMA."""
+    buf = torch.empty(nbytes, dtype=torch.uint8)
+    return buf.pin_memory() if torch.cuda.is_available() else buf
+
+
+def compile_table(site: torch.Tensor, kind: torch.Tensor, coef: torch.Tensor, n_qubytes: int, particle_cut: int,
+                  cache_dir: str | os.PathLike | None = None) -> torch.Tensor:
+    """The compiled term table (host blob) for these terms, read from / written to ``cache_dir`` when given.
+
+    Like qmb/fcidump.py:143-169, which caches the raw (site, kind, coef) table
+    under a checksum of its source, the compiled blob is cached under a
+    SHA-256 of the term tensors, the row width, the particle kind and the
+    library's ABI version; a cached file is used only when qmbx_table_check
+    accepts it (same table format, whole blob), otherwise it is rebuilt.
+    """
+    lib = _native.library()
+    site = site.detach().to("cpu", torch.int16).contiguous()
+    kind = kind.detach().to("cpu", torch.uint8).contiguous()
+    coef = coef.detach().to("cpu", torch.float64).contiguous()
+    if site.dim() != 2 or site.shape[1] != 4 or kind.shape != site.shape or coef.shape != (site.shape[0], 2):
+        raise RuntimeError("site, kind and coef must have shapes [T, 4], [T, 4] and [T, 2]")
+    path = None
+    if cache_dir is not None:
+        h = hashlib.sha256()
+        for t in (site, kind, coef):
+            h.update(t.numpy().tobytes())
+        h.update(struct.pack("<iii", n_qubytes, particle_cut, lib.qmbx_version()))
+        path = os.path.join(os.fspath(cache_dir), f"{h.hexdigest()}.qmbx")
+        if os.path.exists(path):
+            data = np.fromfile(path, dtype=np.uint8)
+            host = _pinned(data.size)
+            host.numpy()[:] = data
+            if lib.qmbx_table_check(host.data_ptr(), host.numel()) == _native.QMBX_OK:
+                return host
+    nbytes = ctypes.c_uint64(0)
+    _native.check(lib.qmbx_table_bytes(site.data_ptr(), kind.data_ptr(), site.shape[0], n_qubytes, particle_cut,
+                                       ctypes.byref(nbytes)))
+    host = _pinned(nbytes.value)
+    _native.check(lib.qmbx_table_build(site.data_ptr(), kind.data_ptr(), coef.data_ptr(), site.shape[0], n_qubytes,
+                                       particle_cut, host.data_ptr(), nbytes.value))
+    if path is not None:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = f"{path}.{os.getpid()}.tmp"
+        host.numpy().tofile(tmp)
+        os.replace(tmp, path)
+    return host
+
+
 class _Table:
     """A compiled term table: host blob (header read by the host) and its device copy."""
 
     def __init__(self, site: torch.Tensor, kind: torch.Tensor, coef: torch.Tensor, n_qubytes: int, particle_cut: int,
-                 device: torch.device):
+                 device: torch.device, cache_dir: str | os.PathLike | None = None):
         lib = _native.library()
-        site = site.detach().to("cpu", torch.int16).contiguous()
-        kind = kind.detach().to("cpu", torch.uint8).contiguous()
-        coef = coef.detach().to("cpu", torch.float64).contiguous()
-        if site.dim() != 2 or site.shape[1] != 4 or kind.shape != site.shape or coef.shape != (site.shape[0], 2):
-            raise RuntimeError("site, kind and coef must have shapes [T, 4], [T, 4] and [T, 2]")
-        nbytes = ctypes.c_uint64(0)
-        _native.check(lib.qmbx_table_bytes(site.data_ptr(), kind.data_ptr(), site.shape[0], n_qubytes, particle_cut,
-                                           ctypes.byref(nbytes)))
-        self.host = torch.empty(nbytes.value, dtype=torch.uint8).pin_memory()
-        _native.check(lib.qmbx_table_build(site.data_ptr(), kind.data_ptr(), coef.data_ptr(), site.shape[0], n_qubytes,
-                                           particle_cut, self.host.data_ptr(), nbytes.value))
-        self.dev = torch.empty(nbytes.value, dtype=torch.uint8, device=device)
+        self.host = compile_table(site, kind, coef, n_qubytes, particle_cut, cache_dir)
+        nbytes = self.host.numel()
+        self.dev = torch.empty(nbytes, dtype=torch.uint8, device=device)
         if self.dev.data_ptr() % 256:
             raise RuntimeError("table allocation is not 256-byte aligned")
         self.dev.copy_(self.host, non_blocking=False)
@@ -98,7 +144,8 @@ class _Table:
 class Hamiltonian:
     """Second-quantized Hamiltonian over bit-packed configurations (see module docstring)."""
 
-    def __init__(self, hamiltonian: dict | tuple[torch.Tensor, torch.Tensor, torch.Tensor], *, kind: str) -> None:
+    def __init__(self, hamiltonian: dict | tuple[torch.Tensor, torch.Tensor, torch.Tensor], *, kind: str,
+                 table_cache: str | os.PathLike | None = None) -> None:
         self.site: torch.Tensor
         self.kind: torch.Tensor
         self.coef: torch.Tensor
@@ -115,6 +162,8 @@ class Hamiltonian:
             case _:
                 raise ValueError(f"Unknown kind: {kind}")
         self._tables: dict = {}
+        # where compiled term tables are cached across processes (compile_table); QMBX_TABLE_CACHE by default
+        self.table_cache = table_cache if table_cache is not None else os.environ.get("QMBX_TABLE_CACHE")
 
     # -- plumbing -----------------------------------------------------------
 
@@ -133,7 +182,7 @@ class Hamiltonian:
         table = self._tables.get(key)
         if table is None:
             with torch.cuda.device(device):
-                table = _Table(self.site, self.kind, self.coef, n_qubytes, self.particle_cut, device)
+                table = _Table(self.site, self.kind, self.coef, n_qubytes, self.particle_cut, device, self.table_cache)
             # tables of this device compiled from other term tensors (or older
             # versions of them) are stale; those for other row widths are kept
             self._tables = {k: v for k, v in self._tables.items() if k[0] != device.index or k[2:] == key[2:]}
@@ -229,6 +278,37 @@ class Hamiltonian:
         """H^dagger applied to g_j on configs_j, restricted to configs_i (the adjoint of apply_within)."""
         return self._apply(configs_i, g_j, configs_j, adjoint=True)
 
+    # -- sparse matrix on a fixed basis ------------------------------------------
+
+    def matrix(self, configs: torch.Tensor, *, max_entries: int | None = None) -> HamiltonianMatrix | None:
+        """H restricted to ``configs`` (distinct rows) as a ``HamiltonianMatrix``.
+
+        Returns None when the matrix would have more than ``max_entries``
+        entries (after the counting walk), so callers can fall back to
+        ``apply_within``.
+        """
+        device = configs.device
+        configs = self._configs(configs, "configs")
+        n = configs.shape[0]
+        table = self._table(device, configs.shape[1])
+        lib = _native.library()
+        need = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_matrix_workspace(table.h, n, ctypes.byref(need)))
+        with torch.cuda.device(device):
+            ws = _workspace(need.value, device)
+            stream = _stream(device)
+            row_ptr = torch.empty(n + 1, dtype=torch.int64, device=device)
+            nnz = ctypes.c_int64(0)
+            _native.call("qmbx_matrix_count", table.h, table.d, configs.data_ptr(), n, row_ptr.data_ptr(),
+                         ctypes.byref(nnz), ws.data_ptr(), ws.numel(), stream)
+            if max_entries is not None and nnz.value > max_entries:
+                return None
+            col = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=device)[:nnz.value]
+            val = torch.empty(max(nnz.value, 1), dtype=torch.complex128, device=device)[:nnz.value]
+            _native.call("qmbx_matrix_fill", table.h, table.d, configs.data_ptr(), n, row_ptr.data_ptr(),
+                         col.data_ptr(), val.data_ptr(), ws.data_ptr(), ws.numel(), stream)
+        return HamiltonianMatrix(row_ptr, col, val)
+
     # -- find_relative --------------------------------------------------------
 
     def find_relative(self, configs_i: torch.Tensor, psi_i: torch.Tensor, count_selected: int,
@@ -272,6 +352,46 @@ class Hamiltonian:
                 raise RuntimeError("find_relative could not size its workspace")
         return out[:n_out.value]
 
+    # -- PT2 step ----------------------------------------------------------------
+
+    def pt2(self, configs: torch.Tensor, psi: torch.Tensor, count_selected: int) -> tuple[float, float, int]:
+        """(E0, E2, rows selected) of the Epstein-Nesbet step of qmb/pert.py:37-61, in one engine call.
+
+        E0 = Re<psi|H|psi>/<psi|psi> on ``configs`` (distinct rows); the
+        connected rows are ``find_relative(configs, psi, count_selected,
+        configs)``; E2 = sum |(H psi)_j|^2 / <psi|psi> / (E0 - Re H_jj) over them.
+        """
+        device = configs.device
+        configs = self._configs(configs, "configs")
+        n = configs.shape[0]
+        psi = self._amplitudes(psi, n, "psi", device).to(torch.complex128)
+        count_selected = int(count_selected)
+        if count_selected <= 0:
+            raise RuntimeError("count_selected must be positive.")
+        table = self._table(device, configs.shape[1])
+        lib = _native.library()
+        need = ctypes.c_uint64(0)
+        _native.check(lib.qmbx_pt2_workspace(table.h, n, count_selected, ctypes.byref(need)))
+        energies = (ctypes.c_double * 2)()
+        n_other = ctypes.c_int64(0)
+        with torch.cuda.device(device):
+            stream = _stream(device)
+            for _ in range(4):
+                ws = _workspace(need.value, device)
+                want = ctypes.c_uint64(0)
+                status = lib.qmbx_pt2(table.h, table.d, configs.data_ptr(), psi.data_ptr(), n, count_selected,
+                                      energies, ctypes.byref(n_other), ws.data_ptr(), ws.numel(), ctypes.byref(want),
+                                      stream)
+                if status == _native.QMBX_ERR_WORKSPACE and want.value > need.value:
+                    need = want
+                    del ws
+                    continue
+                _native.check(status)
+                break
+            else:
+                raise RuntimeError("pt2 could not size its workspace")
+        return energies[0], energies[1], n_other.value
+
     # -- diagonal_term ----------------------------------------------------------
 
     def diagonal_term(self, configs: torch.Tensor) -> torch.Tensor:
@@ -312,6 +432,45 @@ class Hamiltonian:
             _native.call("qmbx_single_relative", table.h, table.d, configs.data_ptr(), configs.shape[0],
                          seed & (2**64 - 1), out.data_ptr(), ws.data_ptr(), ws.numel(), _stream(device))
         return out
+
+
+class HamiltonianMatrix:
+    """H restricted to one set of distinct rows, stored on the device as a sparse matrix (CSR).
+
+    Built by ``Hamiltonian.matrix``: two term walks over the rows (count, then
+    fill); ``apply(x)`` is then a sparse matrix-vector product, which is what
+    an iterative eigensolver on a fixed basis (qmb/rldiag.py:19-52,
+    qmb/haar.py:107-183) needs once per iteration.  Row j holds its diagonal
+    entry first, then one entry per (term, row i) pair mapping row i onto row
+    j.  ``row_ptr`` int64 [n + 1], ``col`` int32 [nnz], ``val`` complex128
+    [nnz].
+    """
+
+    def __init__(self, row_ptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor):
+        self.row_ptr, self.col, self.val = row_ptr, col, val
+        self.n = row_ptr.shape[0] - 1
+        self.nnz = col.shape[0]
+
+    def apply(self, x: torch.Tensor) -> torch.Tensor:
+        """A x for complex128 x on the matrix's rows (bit-identical on every call)."""
+        if x.dtype != torch.complex128 or x.dim() != 1 or x.shape[0] != self.n:
+            raise RuntimeError(f"x must be complex128 of shape [{self.n}].")
+        if x.device != self.val.device:
+            raise RuntimeError("x must be on the matrix's device.")
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        with torch.cuda.device(x.device):
+            _native.call("qmbx_matrix_apply", self.n, self.row_ptr.data_ptr(), self.col.data_ptr(),
+                         self.val.data_ptr(), x.data_ptr(), y.data_ptr(), _stream(x.device))
+        return y
+
+    def to_dense(self) -> torch.Tensor:
+        """The dense matrix (for checks on small row sets)."""
+        rows = torch.repeat_interleave(torch.arange(self.n, device=self.val.device),
+                                       self.row_ptr[1:] - self.row_ptr[:-1])
+        dense = torch.zeros((self.n, self.n), dtype=torch.complex128, device=self.val.device)
+        dense.index_put_((rows, self.col.to(torch.int64)), self.val, accumulate=True)
+        return dense
 
 
 class _ApplyWithin(torch.autograd.Function):
