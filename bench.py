@@ -66,7 +66,8 @@ WORKLOADS = {
     "lanczos": dict(n_orbit=26, n_alpha=7, n_beta=7, n_i=65536, n_j=65536, count_selected=0, seed=2025,
                     lanczos_steps=20,
                     description="ab-initio 52 spin orbitals (n_qubytes 7), 7a+7b, 65536-determinant basis, "
-                                "20 Lanczos iterations"),
+                                "20 Lanczos iterations (H materialised once; through_walks_ms: every iteration "
+                                "walks the terms)"),
     "pt2": dict(n_orbit=38, n_alpha=10, n_beta=10, n_i=8192, n_j=8192, count_selected=1000000, seed=2027,
                 description="ab-initio 76 spin orbitals (n_qubytes 10), 10a+10b, 8192 variational determinants, "
                             "Epstein-Nesbet PT2 over the top 1,000,000 connection records"),
@@ -787,13 +788,23 @@ def run_extra(args, wl) -> dict:
 
         with clocks:
             ms = _timed_loop(run, args.steps, device, flush)
+            ms_walks = _timed_loop(lambda: qmb.lanczos_energy(ham, ci, n_steps, start=start, materialize=False),
+                                   max(1, args.steps // 5), device, flush)
         prof = _profiled(native, run, device)
-        n_apply = prof["groups"]["enumerate"][0]
+        mat = ham.matrix(ci)
+        n_spmv, ms_spmv = prof["groups"]["spmv"]
+        # a product reads every entry (16-byte value, 4-byte column), the row pointers, x through the columns
+        # (at least once per row) and writes y
+        spmv_bytes = mat.nnz * 20 + (n + 1) * 8 + 2 * n * 16
         line.update({"metric": "Lanczos wall time (20 iterations, FP64, Ritz value on the host)", "value": ms,
                      "unit": "ms", "ms_per_step": ms, "higher_is_better": False, "dtype": "f64",
-                     "ms_per_iteration": ms / (n_steps + 2), "energy": result["e"], "walks": n_apply,
-                     "term_applications_per_s": (n_steps + 2) * T * n / (ms * 1e-3),
-                     "roofline": walk_roofline(prof, n, n, 16, "term walk"),
+                     "ms_per_iteration": ms / (n_steps + 2), "energy": result["e"],
+                     "matrix": {"nnz": mat.nnz, "walks_to_build": prof["groups"]["enumerate"][0],
+                                "build_ms": prof["groups"]["enumerate"][1] + prof["groups"]["diagonal"][1],
+                                "products": n_spmv},
+                     "through_walks_ms": ms_walks,
+                     "roofline": hbm_roofline(spmv_bytes, ms_spmv / max(n_spmv, 1),
+                                              "sparse matrix-vector product (spmv_kernel)", None, launches=n_spmv),
                      "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
     elif args.workload == "pt2":
         psi = torch.from_numpy(wl["psi"]).to(device)

@@ -261,16 +261,17 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
 /* ---------------------------------------------------------------------------
  * Tracing (no counterpart in the reference, which has none).
  * Every kernel launch of this library increments a process-wide counter.
- * qmbx_profile_enable(1) additionally brackets the launches of six groups
+ * qmbx_profile_enable(1) additionally brackets the launches of seven groups
  * (0 term walk, 1 key packing/hashing, 2 selection, 3 other, 4 the separate
- * passes over diagonal terms, 5 radix sorts) with CUDA events on the
+ * passes over diagonal terms, 5 radix sorts, 6 products with a materialised
+ * matrix) with CUDA events on the
  * launching stream and resets the totals; qmbx_profile_read waits for the
  * recorded events and returns the launch counter and, per group, the number
  * of timed launches and their total milliseconds (arrays of
  * QMBX_PROFILE_GROUPS).
  * ------------------------------------------------------------------------- */
 
-#define QMBX_PROFILE_GROUPS 6
+#define QMBX_PROFILE_GROUPS 7
 
 int qmbx_profile_enable(int32_t on);
 

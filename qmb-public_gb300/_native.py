@@ -59,7 +59,7 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_profile_read": (ctypes.c_int, [_PI64, _PI64, ctypes.POINTER(ctypes.c_double)]),
 }
 
-PROFILE_GROUPS = ("enumerate", "keys", "select", "other", "diagonal", "sort")
+PROFILE_GROUPS = ("enumerate", "keys", "select", "other", "diagonal", "sort", "spmv")
 
 
 def profile_enable(on: bool) -> None:

@@ -371,7 +371,7 @@ extern "C" int qmbx_matrix_apply(int64_t n, const int64_t* row_ptr, const int32_
         return fail(QMBX_ERR_ARGUMENT, "pointers must not be NULL");
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    QMBX_KERNEL(kGroupEnumerate, s, spmv_kernel<<<grouped_grid(n), kThreads, 0, s>>>(n, row_ptr, col, reinterpret_cast<const double2*>(val), reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y)));
+    QMBX_KERNEL(kGroupSpmv, s, spmv_kernel<<<grouped_grid(n), kThreads, 0, s>>>(n, row_ptr, col, reinterpret_cast<const double2*>(val), reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y)));
     QMBX_LAUNCH_CHECK("spmv_kernel");
     return QMBX_OK;
 }

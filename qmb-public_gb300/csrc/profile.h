@@ -7,7 +7,8 @@ namespace qmbx {
 
 // kGroupEnumerate is the main term walk; kGroupDiagonal the separate
 // passes over diagonal terms that follow it; kGroupSort the radix sorts
-// (histogram, scan and scatter passes)
+// (histogram, scan and scatter passes); kGroupSpmv the products with a
+// materialised matrix
 enum ProfileGroup {
     kGroupEnumerate = 0,
     kGroupKeys = 1,
@@ -15,7 +16,8 @@ enum ProfileGroup {
     kGroupOther = 3,
     kGroupDiagonal = 4,
     kGroupSort = 5,
-    kProfileGroups = 6
+    kGroupSpmv = 6,
+    kProfileGroups = 7
 };
 
 void note_launch(int n);
