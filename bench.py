@@ -7,12 +7,14 @@ determinants with 5 alpha + 5 beta electrons, complex N(0,1) amplitudes.
 
 One step is the FP32-compensated apply_within forward (configs_i ->
 configs_j) followed by its adjoint (configs_j -> configs_i), i.e. the work of
-one energy-gradient evaluation.  The metric is term applications per second
+one energy-gradient evaluation, run as it is in training: through
+apply_within's autograd function, whose forward walk records its hits and
+whose backward replays them.  The metric is term applications per second
 counted as the reference counts them: T * (N_i + N_j) per step (the
 reference's thread grid is T * N_i for a forward application, T * N_j for
-the same kernel run on the daggered table from configs_j).  The walks here
-visit fewer pairs (both directions walk the 20,000 configs_i rows);
-``walked_pairs_per_s`` reports that count, 2 * T * N_i per step.  The same
+the same kernel run on the daggered table from configs_j).  The engine
+visits fewer pairs (one walk over the 20,000 configs_i rows);
+``walked_pairs_per_s`` reports that count.  The same
 line reports the FP64 path, the reference's own CUDA apply_within run from
 its cubin (``ref_cuda_fp64``), find_relative (top 50,000 excluding
 configs_i), the energy error of the FP32 path, the end-to-end rate through
@@ -26,7 +28,7 @@ the forward over a slice of configs_i and the adjoint, as the reference
 would compute it (its apply_within on the daggered table from configs_j
 onto configs_i), over a slice of configs_j, on every host core.
 
-``--workload c1|c3|c4|c5|lanczos|pt2`` runs the other shapes (one JSON line
+``--workload c1|c3|c4|c5|lanczos|pt2|sampler`` runs the other shapes (one JSON line
 each, clocked, L2 flushed before every timed step, with a roofline).
 """
 
@@ -68,6 +70,10 @@ WORKLOADS = {
                     description="ab-initio 52 spin orbitals (n_qubytes 7), 7a+7b, 65536-determinant basis, "
                                 "20 Lanczos iterations (H materialised once; through_walks_ms: every iteration "
                                 "walks the terms)"),
+    "sampler": dict(n_orbit=26, n_alpha=7, n_beta=7, n_i=65536, n_j=65536, count_selected=0, seed=2028,
+                    hidden=(512, 512),
+                    description="autoregressive MLP wave function (qmb/mlp.py WaveFunctionElectronUpDown) on 26 sites "
+                                "(52 spin orbitals), 7a+7b, hidden (512, 512): generate_unique of 65,536 configurations"),
     "pt2": dict(n_orbit=38, n_alpha=10, n_beta=10, n_i=8192, n_j=8192, count_selected=1000000, seed=2027,
                 description="ab-initio 76 spin orbitals (n_qubytes 10), 10a+10b, 8192 variational determinants, "
                             "Epstein-Nesbet PT2 over the top 1,000,000 connection records"),
@@ -311,29 +317,47 @@ def measured_peaks() -> tuple[float, str]:
 KERNEL_SOURCES = ("qmb-public_gb300/csrc/device.cuh", "qmb-public_gb300/csrc/apply.cu",
                   "qmb-public_gb300/csrc/keys.cu", "qmb-public_gb300/csrc/relative.cu",
                   "qmb-public_gb300/csrc/format.h", "qmb-public_gb300/csrc/table.cpp")
+# the sources of the apply_within walks (profiles of grouped_kernel / enumerate_kernel under apply_within)
+APPLY_SOURCES = ("qmb-public_gb300/csrc/device.cuh", "qmb-public_gb300/csrc/apply.cu",
+                 "qmb-public_gb300/csrc/keys.cu", "qmb-public_gb300/csrc/format.h",
+                 "qmb-public_gb300/csrc/table.cpp")
+# the sources of find_relative's walks
+RELATIVE_SOURCES = ("qmb-public_gb300/csrc/device.cuh", "qmb-public_gb300/csrc/relative.cu",
+                    "qmb-public_gb300/csrc/keys.cu", "qmb-public_gb300/csrc/format.h",
+                    "qmb-public_gb300/csrc/table.cpp")
 
 
-def kernel_sources_sha() -> str:
-    """First 16 hex digits of the SHA-256 over the kernel sources (see KERNEL_SOURCES)."""
+def kernel_sources_sha(sources=KERNEL_SOURCES) -> str:
+    """First 16 hex digits of the SHA-256 over kernel source files (paths relative to the repo)."""
     import hashlib
 
     h = hashlib.sha256()
-    for rel in KERNEL_SOURCES:
+    for rel in sources:
         with open(os.path.join(REPO, rel), "rb") as f:
             h.update(f.read())
     return h.hexdigest()[:16]
 
 
+# the committed ncu summary (profiles/<name>.json) of each workload's dominant walk kernel
+WALK_FIGURES = {"c2": "term_walk_c2", "c4": "tiled_walk_c4", "c5": "pivot_walk_c5", "c3": "pivot_walk_c3"}
+
+
 def ncu_figures(name: str) -> dict | None:
     """Per-launch ncu figures committed as profiles/<name>.json, or None when absent or
-    taken on kernel sources other than the current ones (a stale figure is never used)."""
+    taken on kernel sources other than the current ones (a stale figure is never used).
+    The file names the sources its kernel is built from ("sources") and their hash at the
+    capture ("kernel_sources_sha"); without a list, every file of KERNEL_SOURCES counts."""
     path = os.path.join(REPO, "profiles", f"{name}.json")
     try:
         with open(path) as f:
             figs = json.load(f)
     except (OSError, ValueError):
         return None
-    if figs.get("kernel_sources_sha") != kernel_sources_sha():
+    try:
+        current = kernel_sources_sha(tuple(figs.get("sources") or KERNEL_SOURCES))
+    except OSError:
+        return None
+    if figs.get("kernel_sources_sha") != current:
         return None
     return figs
 
@@ -459,14 +483,20 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)  # > 129 MB of L2
     stream = torch.cuda.current_stream(device)
 
-    # the FP32 pipeline: complex64 in and out, compensated accumulation inside
+    # a step is apply_within and its backward (the adjoint applied to the
+    # output, as in an energy-gradient step) through the autograd function:
+    # the forward walk records its hits and the backward replays them.
+    # FP32 pipeline: complex64 in and out, compensated accumulation inside
+    def fwd_adj(psi):
+        p = psi.detach().requires_grad_(True)
+        y = ham.apply_within(ci, p, cj)
+        return torch.autograd.grad(y, p, grad_outputs=y)[0]
+
     def step32():
-        y = ham.apply_within(ci, psi32, cj)
-        return ham.apply_within_adjoint(ci, y, cj)
+        return fwd_adj(psi32)
 
     def step64():
-        y = ham.apply_within(ci, psi64, cj)
-        return ham.apply_within_adjoint(ci, y, cj)
+        return fwd_adj(psi64)
 
     def barrier():
         if world > 1:
@@ -527,10 +557,10 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     def step_e2e():
         a_i = ci_h.to(device, non_blocking=True)
         a_j = cj_h.to(device, non_blocking=True)
-        p = psi_h.to(device, non_blocking=True)
+        p = psi_h.to(device, non_blocking=True).requires_grad_(True)
         y = ham.apply_within(a_i, p, a_j)
-        x = ham.apply_within_adjoint(a_i, y, a_j)
-        y_h.copy_(y, non_blocking=True)
+        (x,) = torch.autograd.grad(y, p, grad_outputs=y)
+        y_h.copy_(y.detach(), non_blocking=True)
         x_h.copy_(x, non_blocking=True)
 
     step_e2e()
@@ -551,6 +581,7 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     stats_rel = native.find_relative_stats()
     native.profile_enable(False)
     n_enum, ms_enum = prof["groups"]["enumerate"]
+    walks_per_step = n_enum / args.steps
 
     if rank != 0:
         return None
@@ -571,11 +602,12 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     # roofline of the term walk: algorithmic bytes per launch
     # forward: targets N_j (key + FP64 result), sources N_i (key + FP32 amplitude), terms T (28 B)
     # adjoint: the same with the two sets swapped
+    # (a step walks once, the forward, when its backward replays the hit log; twice without it)
     alg_fwd = n_j * (nq + 16) + n_i * (nq + 8) + T * 28
     alg_adj = n_i * (nq + 16) + n_j * (nq + 8) + T * 28
-    alg = (alg_fwd + alg_adj) / 2
+    alg = alg_fwd if walks_per_step < 1.5 else (alg_fwd + alg_adj) / 2
     per_launch_ms = ms_enum / max(n_enum, 1)
-    figs = ncu_figures(f"term_walk_{args.workload}")
+    figs = ncu_figures(WALK_FIGURES.get(args.workload, f"term_walk_{args.workload}"))
     ms_step32 = ms32 / args.steps
     value = replica_value(units, ms_step32, world)
     # the radix sorts of find_relative: passes x 2 x records x record bytes over their device time
@@ -602,9 +634,11 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
-        "walked_pairs_per_s": {"value": world * 2 * T * n_i / (ms_step32 * 1e-3),
-                               "what": "(term, row) pairs the walks visit: both directions walk configs_i's "
-                                       f"{n_i} rows, 2 * T * N_i = {2 * T * n_i:.3e} per step"},
+        "walked_pairs_per_s": {"value": world * walks_per_step * T * n_i / (ms_step32 * 1e-3),
+                               "walks_per_step": walks_per_step,
+                               "what": "(term, row) pairs the term walks visit: each walk covers configs_i's "
+                                       f"{n_i} rows (T * N_i = {T * n_i:.3e}); the forward walk records its hits "
+                                       "and the adjoint replays them"},
         "fp64": {"value": world * units / (ms64 / args.steps * 1e-3), "ms_per_step": ms64 / args.steps},
         "speedup_fp32c_vs_fp64": ms64 / ms32,
         "ref_cuda_fp64": ref_cuda,
@@ -707,36 +741,48 @@ def run_extra(args, wl) -> dict:
     def walk_roofline(prof, n_walk, n_look, amp, kernel):
         cnt, ms = prof["groups"]["enumerate"]
         return hbm_roofline(walk_alg(n_walk, n_look, amp), ms / max(cnt, 1), kernel,
-                            ncu_figures(f"term_walk_{args.workload}"), launches=cnt)
+                            ncu_figures(WALK_FIGURES.get(args.workload, f"term_walk_{args.workload}")), launches=cnt)
 
     if args.workload == "c3":
         mlp = _Mlp(8 * nq, device, seed=wl["spec"]["seed"])
 
-        def step(dtype, shortcut=True):
+        def step(dtype, shortcut=True, hit_log=True):
             for p in mlp.net.parameters():
                 p.grad = None
             psi = mlp(ci)
-            e = qmb.variational_energy(ham, ci, psi if dtype == torch.complex64 else psi.to(torch.complex128),
-                                       hermitian_shortcut=shortcut)
-            e.backward()
+            ham.hit_log = hit_log
+            try:
+                e = qmb.variational_energy(ham, ci, psi if dtype == torch.complex64 else psi.to(torch.complex128),
+                                           hermitian_shortcut=shortcut)
+                e.backward()
+            finally:
+                ham.hit_log = True
             return e
 
+        # three backwards: the Hermitian shortcut (default), the forward walk's hit log replayed,
+        # and the adjoint kernel's own walk
         for _ in range(args.warmup):
             step(torch.complex64)
             step(torch.complex128)
             step(torch.complex64, False)
+            step(torch.complex64, False, False)
         with clocks:
             ms32 = _timed_loop(lambda: step(torch.complex64), args.steps, device, flush)
             ms64 = _timed_loop(lambda: step(torch.complex128), args.steps, device, flush)
-            ms32_adj = _timed_loop(lambda: step(torch.complex64, False), args.steps, device, flush)
-            ms64_adj = _timed_loop(lambda: step(torch.complex128, False), args.steps, device, flush)
+            ms32_log = _timed_loop(lambda: step(torch.complex64, False), args.steps, device, flush)
+            ms32_adj = _timed_loop(lambda: step(torch.complex64, False, False), args.steps, device, flush)
+            ms64_adj = _timed_loop(lambda: step(torch.complex128, False, False), args.steps, device, flush)
         prof = _profiled(native, lambda: step(torch.complex64), device)
-        prof_adj = _profiled(native, lambda: step(torch.complex64, False), device)
+        prof_log = _profiled(native, lambda: step(torch.complex64, False), device)
+        prof_adj = _profiled(native, lambda: step(torch.complex64, False, False), device)
         e32 = float(step(torch.complex64).detach())
         e64 = float(step(torch.complex128).detach())
         line.update({"metric": "energy forward + backward step (FP32-compensated)", "value": ms32, "unit": "ms",
                      "ms_per_step": ms32, "higher_is_better": False, "dtype": "f32", "fp64_ms": ms64,
                      "speedup_fp32c_vs_fp64": ms64 / ms32,
+                     "through_hit_log": {"fp32c_ms": ms32_log,
+                                         "walks_per_step": prof_log["groups"]["enumerate"][0],
+                                         "kernel_groups_ms": {g: v[1] for g, v in prof_log["groups"].items()}},
                      "through_adjoint_kernel": {"fp32c_ms": ms32_adj, "fp64_ms": ms64_adj,
                                                 "speedup_fp32c_vs_fp64": ms64_adj / ms32_adj,
                                                 "walks_per_step": prof_adj["groups"]["enumerate"][0],
@@ -750,13 +796,15 @@ def run_extra(args, wl) -> dict:
         psi32 = torch.from_numpy(wl["psi"]).to(torch.complex64).to(device)
         psi64 = psi32.to(torch.complex128)
 
-        def step32():
-            y = ham.apply_within(ci, psi32, cj)
-            return ham.apply_within_adjoint(ci, y, cj)
+        # forward + adjoint as in the headline workload: apply_within's autograd function, whose
+        # backward replays the forward walk's hits
+        def fwd_adj(psi):
+            p = psi.detach().requires_grad_(True)
+            y = ham.apply_within(ci, p, cj)
+            return torch.autograd.grad(y, p, grad_outputs=y)[0]
 
-        def step64():
-            y = ham.apply_within(ci, psi64, cj)
-            return ham.apply_within_adjoint(ci, y, cj)
+        step32 = lambda: fwd_adj(psi32)
+        step64 = lambda: fwd_adj(psi64)
 
         for _ in range(args.warmup):
             step32()
@@ -773,6 +821,7 @@ def run_extra(args, wl) -> dict:
                      "dtype": "f32", "ms_per_step": ms32, "fp64_ms_per_step": ms64,
                      "speedup_fp32c_vs_fp64": ms64 / ms32,
                      "energy_fp64": e64, "energy_fp32c": e32, "energy_abs_error_ha": abs(e32 - e64),
+                     "walks_per_step": prof["groups"]["enumerate"][0],
                      "roofline": walk_roofline(prof, n, cj.shape[0], 8, "term walk"),
                      "kernel_groups_ms_per_step": {g: v[1] for g, v in prof["groups"].items()}})
     elif args.workload == "lanczos":
@@ -824,6 +873,39 @@ def run_extra(args, wl) -> dict:
                      "higher_is_better": False, "dtype": "f64", "count_selected": K, "e0": result["e"][0],
                      "e2": result["e"][1],
                      "roofline": walk_roofline(prof, n, n, 16, "term walk"),
+                     "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
+    elif args.workload == "sampler":
+        from oracle import sampler as oracle_sampler
+
+        spec = wl["spec"]
+        sites = spec["n_orbit"]
+        torch.manual_seed(spec["seed"])
+        net = qmb.sampler.WaveFunctionElectronUpDown(double_sites=2 * sites, physical_dim=2, is_complex=True,
+                                                     spin_up=spec["n_alpha"], spin_down=spec["n_beta"],
+                                                     hidden_size=spec["hidden"], ordering=+1).to(device)
+        params = {k: v.detach() for k, v in net.state_dict().items()}
+        batch = spec["n_i"]
+        for _ in range(args.warmup):
+            net.generate_unique(batch)
+        out = {}
+
+        def run():
+            out["n"] = net.generate_unique(batch)[0].shape[0]
+
+        def run_ref():
+            oracle_sampler.generate_unique(params, sites, spec["n_alpha"], spec["n_beta"], batch,
+                                           lambda site, rows: torch.rand((rows, 4), device=device))
+
+        run_ref()
+        with clocks:
+            ms = _timed_loop(run, args.steps, device, flush)
+            ms_ref = _timed_loop(run_ref, max(1, args.steps // 2), device, flush)
+        prof = _profiled(native, run, device)
+        line.update({"metric": "generate_unique wall time (65,536 configurations)", "value": ms, "unit": "ms",
+                     "ms_per_step": ms, "higher_is_better": False, "dtype": "f32", "rows_out": out["n"],
+                     "reference_algorithm_torch_ms": ms_ref, "speedup_vs_reference_algorithm": ms_ref / ms,
+                     "reference_algorithm": "oracle/sampler.py: the reference's generate_unique restated in plain "
+                                            "torch (pinned to the reference's own outputs), same GPU, same network",
                      "kernel_groups_ms_per_run": {g: v[1] for g, v in prof["groups"].items()}})
     else:  # c5: find_relative
         psi = torch.from_numpy(wl["psi"]).to(device)
@@ -925,7 +1007,7 @@ def main():
 
     import torch
 
-    if args.workload in ("c1", "c3", "c4", "c5", "lanczos", "pt2"):
+    if args.workload in ("c1", "c3", "c4", "c5", "lanczos", "pt2", "sampler"):
         if rank == 0:
             print(json.dumps(run_extra(args, make_workload(args.workload))), flush=True)
         return

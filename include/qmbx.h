@@ -81,8 +81,14 @@ int qmbx_table_counts(const void* table_host, int64_t counts[6]);
  * the daggered, conjugated terms closed form by closed form (1e-12 relative
  * to the largest coefficient) and requires the diagonal terms to sum to real
  * coefficients; an operator written so that equal matrices have different
- * closed forms can be reported 0 although Hermitian, never the reverse.
- * Callers use it to get the gradient of <psi|H|psi> from H psi alone. */
+ * closed forms can be reported 0 although Hermitian.  The tolerance is the
+ * bound the other way: an operator whose closed forms differ from their
+ * adjoints' by at most 1e-12 of the largest |coefficient| is reported 1, and
+ * a gradient taken from H psi alone then misses that anti-Hermitian part
+ * (its size is at most 1e-12 max|c| times the number of such terms).
+ * Callers use it to get the gradient of <psi|H|psi> from H psi alone; the
+ * Python energy function takes hermitian_shortcut=False to always walk the
+ * adjoint instead. */
 int qmbx_table_hermitian(const void* table_host, int32_t* hermitian);
 
 /* ---------------------------------------------------------------------------
@@ -92,6 +98,17 @@ int qmbx_table_hermitian(const void* table_host, int32_t* hermitian);
  * first occurrence receives the amplitude and the others zero.
  * same_configs != 0 declares configs_i and configs_j to be the same rows
  * (configs_j is then ignored), which saves one sort.
+ *
+ * Determinism (this entry point, its adjoint and their FP32 variants): the
+ * walk over the output side's rows sums each row in a fixed order and
+ * repeats bit for bit; it is taken when the rows are the same or the output
+ * side is not much larger than the input side.  Otherwise the input side is
+ * walked and contributions are added with FP64 atomics (as is every
+ * pivot-major walk, taken for tables whose pivot groups hold hundreds of
+ * terms), whose order varies from run to run in the last bits.
+ * QMBX_DETERMINISTIC=1 in the environment (read at every call) keeps every
+ * call on the fixed-order walk.  Repeated rows of an input are summed with
+ * atomics before the walk in any case.
  * ------------------------------------------------------------------------- */
 
 int qmbx_apply_within_workspace(const void* table_host, int64_t n_i, int64_t n_j, uint64_t* bytes);
@@ -183,6 +200,57 @@ int qmbx_matrix_fill(const void* table_host, const void* table_dev, const uint8_
 int qmbx_matrix_apply(int64_t n, const int64_t* row_ptr, const int32_t* col, const double* val, const double* x,
                       double* y, qmbx_stream_t stream);
 
+/* Y = A X for m complex128 vectors at once (X, Y row-major [n][m]; m = 1 is a
+ * plain product), given the matrix's entry count nnz (row_ptr[n]).  Every
+ * call with the same arguments gives the same bits: each output is summed
+ * over its row's entries in order (rows averaging fewer than 4 entries and
+ * m = 1: a thread per row; otherwise a warp per row). */
+int qmbx_matrix_apply_many(int64_t n, int64_t nnz, int32_t m, const int64_t* row_ptr, const int32_t* col,
+                           const double* val, const double* x, double* y, qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Hit logs (no counterpart in the reference): a forward apply_within that
+ * also records what its walk found, and the adjoint product on the same rows
+ * computed from that record without a second walk -- the backward of an
+ * energy gradient needs exactly the (term, row) pairs the forward found.
+ * qmbx_hitlog_bytes sizes the caller's log buffer (device, 256-byte aligned)
+ * for n_i x n_j rows and log_cap hit records (16 bytes each).  The _logged
+ * forwards take the same arguments as qmbx_apply_within /
+ * qmbx_apply_within_f32c plus the log; the _logged adjoints take the log,
+ * the same table and row counts, and g_j, and give what
+ * qmbx_apply_within_adjoint(_f32c) gives (include_diagonal as in the
+ * forward).  An adjoint call synchronises the stream to read the hit count;
+ * when the forward found more hits than log_cap it returns
+ * QMBX_ERR_WORKSPACE with the count in *hits_needed (a caller then runs
+ * qmbx_apply_within_adjoint(_f32c), or a larger log next time).  The log's
+ * header keeps the forward's n_i, n_j (n_i when same_configs was set) and
+ * log_cap; an adjoint call with other values, or on a buffer no logged
+ * forward wrote, returns QMBX_ERR_ARGUMENT before reading the records.  The
+ * adjoint adds with FP64 atomics (not bitwise repeatable).
+ * ------------------------------------------------------------------------- */
+
+int qmbx_hitlog_bytes(int64_t n_i, int64_t n_j, int64_t log_cap, uint64_t* bytes);
+
+int qmbx_apply_within_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                             const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                             int32_t same_configs, double* psi_j, void* workspace, uint64_t workspace_bytes, void* log,
+                             uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream);
+
+int qmbx_apply_within_f32c_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                  const float* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                                  int32_t same_configs, int32_t include_diagonal, double* out_f64, float* out_f32,
+                                  void* workspace, uint64_t workspace_bytes, void* log, uint64_t log_bytes,
+                                  int64_t log_cap, qmbx_stream_t stream);
+
+int qmbx_apply_within_adjoint_logged(const void* table_host, const void* table_dev, const void* log,
+                                     uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j, const double* g_j,
+                                     double* out_i, int64_t* hits_needed, qmbx_stream_t stream);
+
+int qmbx_apply_within_adjoint_f32c_logged(const void* table_host, const void* table_dev, const void* log,
+                                          uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
+                                          const float* g_j, double* out_f64, float* out_f32, int64_t* hits_needed,
+                                          qmbx_stream_t stream);
+
 /* ---------------------------------------------------------------------------
  * diagonal_term: out[c] = sum of s * coef_t over terms with t|c> = s|c>.
  * Replaces diagonal_term_interface (qmb/_hamiltonian_cuda.cu:710-803).
@@ -259,12 +327,57 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
                          qmbx_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * The elementwise parts of the autoregressive network of qmb/mlp.py:60-314
+ * (WaveFunctionElectronUpDown, the caller that samples the configurations
+ * the engine works on).  The site networks' matrix products stay with the
+ * caller (cuBLAS); these kernels do what lies between them.  A site's four
+ * entries k = 2 up + down; counts are (up, down) electrons so far; FP32 as
+ * the reference's network.
+ *
+ * qmbx_sampler_log_amplitude: total[r] = sum over sites i of the masked,
+ * normalised log amplitude deltas[i][r][occ[r][i]] (replaces the site loop
+ * of the reference's forward, :188-205); deltas float [sites][rows][4], occ
+ * uint8 [rows][sites], total double [rows].  _grad: d total / d deltas
+ * times grad (double [rows]) into grad_deltas (float [sites][rows][4]).
+ *
+ * qmbx_sampler_site: one site of generate_unique (:232-266) for n partial
+ * rows: from delta float [n][4], counts int32 [n][2], the rows' log
+ * probability lp and Gumbel value gp (float [n]) and uniforms float [n][4],
+ * the children's log probabilities l_out and conditioned Gumbel values
+ * t_out (float [4][n], child k of row r at k n + r, the reference's order).
+ * Optionally (both or neither) la, the rows' log amplitudes so far (double
+ * [n]), and a_out (double [4][n]): each child's la + its normalised log
+ * amplitude -- after the last site, the log amplitude the forward gives the
+ * configuration, so psi needs only the phase network.
+ * qmbx_sampler_take: the m chosen children (index int64 [m] into [4][n]):
+ * occupations occ_out uint8 [m][sites] from occ_in, network inputs xf_out
+ * float [m][2 sites] (sites up to `site` written), counts, lp, gp, and
+ * (optionally, both or neither) la_out from a_in.
+ * ------------------------------------------------------------------------- */
+
+int qmbx_sampler_log_amplitude(int64_t rows, int32_t sites, int32_t spin_up, int32_t spin_down, const float* deltas,
+                               const uint8_t* occ, double* total, qmbx_stream_t stream);
+
+int qmbx_sampler_log_amplitude_grad(int64_t rows, int32_t sites, int32_t spin_up, int32_t spin_down,
+                                    const float* deltas, const uint8_t* occ, const double* grad, float* grad_deltas,
+                                    qmbx_stream_t stream);
+
+int qmbx_sampler_site(int64_t n, int32_t site, int32_t sites, int32_t spin_up, int32_t spin_down, const float* delta,
+                      const int32_t* counts, const float* lp, const float* gp, const float* uniforms, float* l_out,
+                      float* t_out, const double* la, double* a_out, qmbx_stream_t stream);
+
+int qmbx_sampler_take(int64_t m, int64_t n, int32_t site, int32_t sites, const int64_t* index, const uint8_t* occ_in,
+                      const int32_t* counts_in, const float* l_in, const float* t_in, uint8_t* occ_out, float* xf_out,
+                      int32_t* counts_out, float* lp_out, float* gp_out, const double* a_in, double* la_out,
+                      qmbx_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Tracing (no counterpart in the reference, which has none).
  * Every kernel launch of this library increments a process-wide counter.
  * qmbx_profile_enable(1) additionally brackets the launches of seven groups
  * (0 term walk, 1 key packing/hashing, 2 selection, 3 other, 4 the separate
  * passes over diagonal terms, 5 radix sorts, 6 products with a materialised
- * matrix) with CUDA events on the
+ * matrix or replayed from a hit log) with CUDA events on the
  * launching stream and resets the totals; qmbx_profile_read waits for the
  * recorded events and returns the launch counter and, per group, the number
  * of timed launches and their total milliseconds (arrays of

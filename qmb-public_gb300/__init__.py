@@ -5,9 +5,9 @@
 in hand-written sm_103a CUDA kernels behind the C ABI of include/qmbx.h.
 """
 
-from . import bitspack, terms  # noqa: F401
+from . import bitspack, sampler, terms  # noqa: F401
 from .energy import variational_energy  # noqa: F401
 from .hamiltonian import Hamiltonian, HamiltonianMatrix  # noqa: F401
 from .solvers import lanczos_energy, pt2_energy  # noqa: F401
 
-__all__ = ["Hamiltonian", "HamiltonianMatrix", "variational_energy", "lanczos_energy", "pt2_energy", "bitspack", "terms"]
+__all__ = ["Hamiltonian", "HamiltonianMatrix", "variational_energy", "lanczos_energy", "pt2_energy", "bitspack", "sampler", "terms"]

@@ -128,10 +128,19 @@ struct GatherF64 : VisitorBase {
     const double2* dcoef;    // coefficients of the diagonal part
     const int32_t* unique;   // walk index -> first row of the walked key
     double2* res;            // result per first row of the walked side
+    HitLog log;              // optional record of the hits (for the adjoint without a walk)
     struct Acc {
         double re, im, dre, dim;
+        int row;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const { a.re = a.im = a.dre = a.dim = 0.0; }
+    __device__ __forceinline__ void init(Acc& a, int64_t u, const Key<W>&, int*) const {
+        a.re = a.im = a.dre = a.dim = 0.0;
+        a.row = __ldg(unique + u);
+    }
+    __device__ __forceinline__ void record_hits(const Acc& a, const int2* q, int n, int lane) const {
+        log_hits(log, a.row, q, n, lane);
+    }
+    __device__ __forceinline__ void record_hit(const Acc& a, int2 h) const { log_hit(log, a.row, h); }
     static constexpr bool kBatched = true;
     static constexpr bool kProbe = true;
     __device__ __forceinline__ bool take(Acc&, const Key<W>&, const Key<W>&, int parity, int64_t slot, int64_t pos,
@@ -160,7 +169,10 @@ struct GatherF64 : VisitorBase {
     }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
         int2 h;
-        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
+        if (probe(a, c, img, parity, slot, h)) {
+            record_hit(a, h);
+            apply_hit(a, h);
+        }
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         double2 cf = __ldg(dcoef + slot);
@@ -177,6 +189,7 @@ struct GatherF64 : VisitorBase {
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         if (a.dre != 0.0 || a.dim != 0.0) {
             int64_t pos = hash_find<W>(lookup, c);
+            if (pos >= 0) log_diag(log, u, a.row, pos, a.dre, CONJ ? -a.dim : a.dim);
             if (pos >= 0) {
                 double2 p = __ldg(val + pos);
                 a.re += a.dre * p.x - a.dim * p.y;
@@ -203,15 +216,22 @@ struct GatherF32C : VisitorBase {
     int include_diag;
     const int32_t* unique;
     double2* res;
+    HitLog log;
     struct Acc {
         CompSum re, im, dre, dim;
+        int row;
     };
-    __device__ __forceinline__ void init(Acc& a, int64_t, const Key<W>&, int*) const {
+    __device__ __forceinline__ void init(Acc& a, int64_t u, const Key<W>&, int*) const {
         a.re.zero();
         a.im.zero();
         a.dre.zero();
         a.dim.zero();
+        a.row = __ldg(unique + u);
     }
+    __device__ __forceinline__ void record_hits(const Acc& a, const int2* q, int n, int lane) const {
+        log_hits(log, a.row, q, n, lane);
+    }
+    __device__ __forceinline__ void record_hit(const Acc& a, int2 h) const { log_hit(log, a.row, h); }
     static constexpr bool kBatched = true;
     static constexpr bool kProbe = true;
     __device__ __forceinline__ bool take(Acc&, const Key<W>&, const Key<W>&, int parity, int64_t slot, int64_t pos,
@@ -229,7 +249,10 @@ struct GatherF32C : VisitorBase {
     }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
         int2 h;
-        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
+        if (probe(a, c, img, parity, slot, h)) {
+            record_hit(a, h);
+            apply_hit(a, h);
+        }
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         comp_diag_add<CONJ>(a.dre, a.dim, __ldg(dcoef32 + slot), parity);
@@ -245,6 +268,7 @@ struct GatherF32C : VisitorBase {
         const double dre = a.dre.value(), dim = a.dim.value();
         if (include_diag && (dre != 0.0 || dim != 0.0)) {
             int64_t pos = hash_find<W>(lookup, c);
+            if (pos >= 0) log_diag(log, u, a.row, pos, dre, CONJ ? -dim : dim);
             if (pos >= 0) {
                 float2 p = __ldg(val + pos);
                 re += dre * (double)p.x - dim * (double)p.y;
@@ -298,13 +322,20 @@ struct Scatter : VisitorBase {
     const float4* dcoef32;  // diagonal part, hi/lo FP32 (F32 path)
     int include_diag;
     double2* acc;           // per unique output-side key
+    HitLog log;
     struct Acc {
         double2 p;
         double dre, dim;    // FP64 path
         CompSum fre, fim;   // F32 path
+        int row;
     };
+    __device__ __forceinline__ void record_hits(const Acc& a, const int2* q, int n, int lane) const {
+        log_hits(log, a.row, q, n, lane);
+    }
+    __device__ __forceinline__ void record_hit(const Acc& a, int2 h) const { log_hit(log, a.row, h); }
     __device__ __forceinline__ void init(Acc& a, int64_t u, const Key<W>&, int*) const {
         const int64_t row = __ldg(unique + u);
+        a.row = (int)row;
         if (F32) {
             float2 q = __ldg(static_cast<const float2*>(val) + row);
             a.p = make_double2((double)q.x, (double)q.y);
@@ -360,7 +391,10 @@ struct Scatter : VisitorBase {
     }
     __device__ __forceinline__ void visit(Acc& a, const Key<W>& c, const Key<W>& img, int parity, int64_t slot) const {
         int2 h;
-        if (probe(a, c, img, parity, slot, h)) apply_hit(a, h);
+        if (probe(a, c, img, parity, slot, h)) {
+            record_hit(a, h);
+            apply_hit(a, h);
+        }
     }
     __device__ __forceinline__ void visit_diag(Acc& a, const Key<W>&, int parity, int64_t slot) const {
         if (F32) {
@@ -381,11 +415,12 @@ struct Scatter : VisitorBase {
             a.dim = warp_sum(a.dim);
         }
     }
-    __device__ __forceinline__ void finish(Acc& a, int64_t, const Key<W>& c) const {
+    __device__ __forceinline__ void finish(Acc& a, int64_t w, const Key<W>& c) const {
         const double dre = F32 ? a.fre.value() : a.dre, dim = F32 ? a.fim.value() : a.dim;
         if (!include_diag || (dre == 0.0 && dim == 0.0)) return;
         int64_t u = hash_find<W>(lookup, c);
         if (u < 0) return;
+        log_diag(log, w, a.row, u, dre, dim);
         atomicAdd(&acc[u].x, dre * a.p.x - dim * a.p.y);
         atomicAdd(&acc[u].y, dre * a.p.y + dim * a.p.x);
     }
@@ -405,7 +440,18 @@ struct PivotHits : VisitorBase {
     const double2* coef;
     const float4* coef32;
     double2* res;
+    HitLog log;
     struct Acc {};
+    __device__ __forceinline__ void record_row_hits(const int4* q, int n, int lane) const {
+        if (log.hits == nullptr || n <= 0) return;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(log.count, (unsigned long long)n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < n && base + lane < (unsigned long long)log.cap) {
+            const int4 h = q[lane];
+            log.hits[base + lane] = make_int4(__ldg(unique + h.z), h.y, h.x, 0);
+        }
+    }
     __device__ __forceinline__ bool probe_row(const Key<W>&, const Key<W>& img, int parity, int64_t slot, int64_t u,
                                               int4& h) const {
         const int64_t pos = hash_find<W>(lookup, img);
@@ -460,6 +506,7 @@ struct DiagAdd : VisitorBase {
     const double2* dcoef;    // FP64 path
     const float4* dcoef32;   // F32 path (hi/lo)
     double2* res;
+    HitLog log;
     struct Acc {
         double dre, dim;     // FP64 path
         CompSum fre, fim;    // F32 path
@@ -497,6 +544,7 @@ struct DiagAdd : VisitorBase {
         if (a.dre == 0.0 && a.dim == 0.0) return;
         const int64_t pos = hash_find<W>(lookup, c);
         if (pos < 0) return;
+        log_diag(log, u, __ldg(unique + u), pos, a.dre, a.dim);
         const int64_t from = SCATTER ? (int64_t)__ldg(unique + u) : pos;
         const int64_t to = SCATTER ? pos : (int64_t)__ldg(unique + u);
         double px, py;
@@ -513,6 +561,25 @@ struct DiagAdd : VisitorBase {
         atomicAdd(&res[to].y, a.dre * py + a.dim * px);
     }
 };
+
+// The first 32 bytes of a hit log: written by the forward call, checked by
+// the replay before it reads anything else.
+struct LogHead {
+    unsigned long long count;  // hits found (more than the capacity: the log is incomplete)
+    int32_t dir;               // 0: walked the input side, 1: the output side, 2: nothing walked
+    int32_t magic;
+    int64_t n_i, n_j;          // the forward call's row counts (n_j = n_i for same_configs)
+    int64_t cap;               // and its capacity in hits
+};
+constexpr int32_t kLogMagic = 0x51484c47;
+
+__global__ void log_head_kernel(LogHead* h, int dir, int64_t n_i, int64_t n_j, int64_t cap) {
+    h->dir = dir;
+    h->magic = kLogMagic;
+    h->n_i = n_i;
+    h->n_j = n_j;
+    h->cap = cap;
+}
 
 // Write the user's output rows from the per-first-row results: the forward
 // map gives each key's value to its first row only (repeated rows get zero),
@@ -567,6 +634,10 @@ struct ApplyArgs {
     double2* out64;   // forward: n_j rows; adjoint: n_i rows
     float2* out32;
     int include_diag;
+    HitLog log;       // forward calls: record the hits here (hits == NULL: no record)
+    LogHead* log_head;   // and the walk's direction and row counts
+    int32_t* log_first;  // and, per configs_i row, its first row
+    int64_t log_rows;    // diagonal records the replay reads: max(n_i, n_j)
 };
 
 // Launch one enumeration over the unique rows of `walk`: the grouped kernel
@@ -634,6 +705,11 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         return fail(QMBX_ERR_WORKSPACE, "workspace of %llu bytes is smaller than the %llu needed",
                     (unsigned long long)ws.cap, (unsigned long long)ws.used);
     }
+    if (a.log.hits != nullptr) {
+        // an empty record until the walk below fills it (direction 2: nothing walked)
+        QMBX_CUDA_TRY(cudaMemsetAsync(a.log.count, 0, sizeof(unsigned long long), s));
+        QMBX_KERNEL(kGroupOther, s, log_head_kernel<<<1, 1, 0, s>>>(a.log_head, 2, a.n_i, a.n_j, a.log.cap));
+    }
     if (n_out == 0) return QMBX_OK;
     int st;
     if (n_in == 0) {
@@ -677,6 +753,15 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     const bool pivot = kind == Walk::kPivot;
     if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
     const HashView look = scatter ? out_set.hash() : in_set.hash();
+    if (a.log.hits != nullptr) {
+        // the record of this forward call: no diagonal records yet, the walk's
+        // direction and configs_i's first rows (the adjoint's output map)
+        // (every record the replay reads, not only the walked side's: the
+        // replay runs over max(n_i, n_j) of them)
+        QMBX_CUDA_TRY(cudaMemsetAsync(a.log.diag_rows, 0xff, (size_t)a.log_rows * sizeof(int2), s));
+        QMBX_KERNEL(kGroupOther, s, log_head_kernel<<<1, 1, 0, s>>>(a.log_head, scatter ? 0 : 1, a.n_i, a.n_j, a.log.cap));
+        QMBX_CUDA_TRY(cudaMemcpyAsync(a.log_first, rs_i.first, (size_t)a.n_i * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    }
     // the grouped kernel walks the changing terms and a tiled pass adds the
     // diagonal ones
     const bool grouped = kind == Walk::kGrouped;
@@ -685,8 +770,8 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     if (pivot) {
 #define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
     {                                                                                                            \
-        PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res};             \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res};                           \
+        PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res}; v.log = a.log;             \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;                           \
         st = launch_pivot<W>(v, dv, walk, part, diag, s);                                                        \
     }
         const bool f32 = a.prec == Prec::F32C;
@@ -707,36 +792,36 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
     } else if (scatter) {
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
-                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res};
+                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res};
+                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         } else {
             if (a.adjoint) {
-                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res};
+                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res};
+                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
     } else {
         if (a.prec == Prec::F64) {
             if (a.adjoint) {
-                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
+                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res};
+                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         } else {
             if (a.adjoint) {
-                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res};
+                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             } else {
-                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res};
+                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
                 st = launch_walk<W>(v, walk, part, walk_diag, s);
             }
         }
@@ -746,7 +831,7 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         const bool f32 = a.prec == Prec::F32C;
 #define QMBX_DIAG_CASE(CONJ, F32, SCATTER)                                              \
     {                                                                                   \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res};  \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;  \
         st = launch_diag<W>(dv, walk, part, diag, s);                                   \
     }
         if (scatter) {
@@ -926,4 +1011,280 @@ extern "C" int qmbx_diagonal_term(const void* table_host, const void* table_dev,
         case 4: return diagonal_impl<4>(table_host, table_dev, configs, n, o, s);
         default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
     }
+}
+
+// ---------------------------------------------------------------------------
+// Hit logs: a forward apply_within that records what its walk found, and the
+// adjoint product computed from that record instead of a second walk.  In an
+// energy-gradient step the adjoint follows the forward on the same rows (the
+// backward of apply_within), and every (term, row) pair it needs is one the
+// forward walk already found; replaying the record reads ~16 bytes per hit
+// instead of testing every term of every walked row again.
+//
+// Log layout (one caller buffer, 256-byte aligned): a 256-byte header
+// (LogHead: hit count, walk direction, the forward's row counts and
+// capacity), configs_i's first rows (n_i int32), the
+// per-walk-index diagonal records (max(n_i, n_j) int2 + double2), the
+// adjoint's per-first-row sums (n_i double2), then cap hit records (int4).
+// ---------------------------------------------------------------------------
+
+namespace qmbx {
+namespace {
+
+struct LogLayout {
+    uint64_t count, dir, first, diag_rows, diag_val, res, hits, total;
+};
+
+LogLayout log_layout(int64_t n_i, int64_t n_j, int64_t cap) {
+    LogLayout L;
+    Arena a(nullptr, 0);
+    L.count = 0;  // LogHead at the start of the header
+    L.dir = offsetof(LogHead, dir);
+    a.take<unsigned char>(256);
+    const uint64_t nw = (uint64_t)(n_i > n_j ? n_i : n_j);
+    L.first = a.used;
+    a.take<int32_t>((uint64_t)(n_i > 0 ? n_i : 1));
+    L.diag_rows = a.used;
+    a.take<int2>(nw > 0 ? nw : 1);
+    L.diag_val = a.used;
+    a.take<double2>(nw > 0 ? nw : 1);
+    L.res = a.used;
+    a.take<double2>((uint64_t)(n_i > 0 ? n_i : 1));
+    L.hits = a.used;
+    a.take<int4>((uint64_t)(cap > 0 ? cap : 1));
+    L.total = a.used;
+    return L;
+}
+
+int attach_log(ApplyArgs& a, void* log, uint64_t log_bytes, int64_t cap) {
+    if (log == nullptr || reinterpret_cast<uintptr_t>(log) % QMBX_ALIGN != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "log must be a %d-byte aligned device buffer", QMBX_ALIGN);
+    }
+    if (cap < 0) return fail(QMBX_ERR_ARGUMENT, "log capacity must not be negative");
+    const int64_t n_j = a.same ? a.n_i : a.n_j;
+    const LogLayout L = log_layout(a.n_i, n_j, cap);
+    if (log_bytes < L.total) {
+        return fail(QMBX_ERR_WORKSPACE, "a log of %lld hits on %lld x %lld rows needs %llu bytes", (long long)cap,
+                    (long long)a.n_i, (long long)n_j, (unsigned long long)L.total);
+    }
+    char* b = static_cast<char*>(log);
+    a.log.hits = reinterpret_cast<int4*>(b + L.hits);
+    a.log.count = reinterpret_cast<unsigned long long*>(b + L.count);
+    a.log.cap = cap;
+    a.log.diag_rows = reinterpret_cast<int2*>(b + L.diag_rows);
+    a.log.diag_val = reinterpret_cast<double2*>(b + L.diag_val);
+    a.log_head = reinterpret_cast<LogHead*>(b);
+    a.log_first = reinterpret_cast<int32_t*>(b + L.first);
+    a.log_rows = a.n_i > n_j ? a.n_i : n_j;
+    return QMBX_OK;
+}
+
+// res[out] += conj(s * coef) * g[in] for every recorded hit: out and in are
+// the walked and the looked-up rows (direction 0: the forward walked the
+// input side) or the reverse (direction 1); the coefficient is read from the
+// part the forward walked.  A drain of the forward writes up to 32
+// consecutive records of one walked row, so when the walked rows are the
+// outputs (direction 0) neighbouring lanes add into the same row: each warp
+// first sums its runs of equal output rows (a segmented shuffle scan) and
+// the last lane of a run adds the run's sum, one atomic pair per run instead
+// of one per record.  Lanes past n take part in the scan with nothing to add.
+template <bool F32>
+__global__ void log_adjoint_kernel(const int4* __restrict__ hits, int64_t n, const int* __restrict__ dir_p,
+                                   PartView fwd, PartView adj, const void* __restrict__ g,
+                                   double2* __restrict__ res) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= n) return;  // whole warps past n
+    const int lane = threadIdx.x & 31;
+    const bool live = i < n;
+    const int dir = *dir_p;
+    const int4 h = live ? hits[i] : make_int4(-1, -1, 0, 0);
+    const int64_t slot = h.z & 0x7fffffff;
+    const int out = dir == 0 ? h.x : h.y;
+    const int in = dir == 0 ? h.y : h.x;
+    double re = 0.0, im = 0.0;
+    if (!live) {
+    } else if (F32) {
+        const float4 cf = __ldg((dir == 0 ? fwd.coef32 : adj.coef32) + slot);
+        const float2 p = __ldg(static_cast<const float2*>(g) + in);
+        // conj(c) p with c = (cf.x + cf.y) + i (cf.z + cf.w): exact FP32 two-products, summed in FP64
+        float x1, e1, x2, e2;
+        two_prod(cf.x, p.x, x1, e1);
+        two_prod(cf.z, p.y, x2, e2);
+        float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fmul_rn(cf.y, p.x), __fmul_rn(cf.w, p.y)));
+        re = ((double)x1 + (double)x2) + (double)lo;
+        two_prod(cf.x, p.y, x1, e1);
+        two_prod(cf.z, p.x, x2, e2);
+        lo = __fadd_rn(__fsub_rn(e1, e2), __fsub_rn(__fmul_rn(cf.y, p.y), __fmul_rn(cf.w, p.x)));
+        im = ((double)x1 - (double)x2) + (double)lo;
+    } else {
+        const double2 cf = __ldg((dir == 0 ? fwd.coef : adj.coef) + slot);
+        const double2 p = __ldg(static_cast<const double2*>(g) + in);
+        re = cf.x * p.x + cf.y * p.y;
+        im = cf.x * p.y - cf.y * p.x;
+    }
+    if (h.z < 0) {
+        re = -re;
+        im = -im;
+    }
+    // runs of equal `out` in lane order: run index = number of run heads up to this lane
+    const unsigned full = 0xffffffffu;
+    const int prev = __shfl_up_sync(full, out, 1);
+    const unsigned heads = __ballot_sync(full, lane == 0 || prev != out);
+    const int run = __popc(heads & (full >> (31 - lane)));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const double r = __shfl_up_sync(full, re, off);
+        const double m = __shfl_up_sync(full, im, off);
+        const int k = __shfl_up_sync(full, run, off);
+        if (lane >= off && k == run) {
+            re += r;
+            im += m;
+        }
+    }
+    const int next = __shfl_down_sync(full, run, 1);
+    if (live && (lane == 31 || next != run)) {
+        atomicAdd(&res[out].x, re);
+        atomicAdd(&res[out].y, im);
+    }
+}
+
+template <bool F32>
+__global__ void log_diag_adjoint_kernel(const int2* __restrict__ rows, const double2* __restrict__ vals, int64_t n,
+                                        const int* __restrict__ dir_p, const void* __restrict__ g,
+                                        double2* __restrict__ res) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 d = rows[i];
+    if (d.y < 0) return;
+    const int dir = *dir_p;
+    const int out = dir == 0 ? d.x : d.y;
+    const int in = dir == 0 ? d.y : d.x;
+    const double2 v = vals[i];
+    double px, py;
+    if (F32) {
+        const float2 q = __ldg(static_cast<const float2*>(g) + in);
+        px = q.x;
+        py = q.y;
+    } else {
+        const double2 q = __ldg(static_cast<const double2*>(g) + in);
+        px = q.x;
+        py = q.y;
+    }
+    atomicAdd(&res[out].x, v.x * px + v.y * py);
+    atomicAdd(&res[out].y, v.x * py - v.y * px);
+}
+
+int adjoint_from_log(const void* table_host, const void* table_dev, const void* log, uint64_t log_bytes, int64_t cap,
+                     int64_t n_i, int64_t n_j, bool f32, const void* g, double2* out64, float2* out32,
+                     int64_t* hits_needed, cudaStream_t s) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if (n_i < 0 || n_j < 0 || n_i >= (int64_t(1) << 31) || n_j >= (int64_t(1) << 31)) {
+        return fail(QMBX_ERR_ARGUMENT, "row counts out of range");
+    }
+    if (log == nullptr || reinterpret_cast<uintptr_t>(log) % QMBX_ALIGN != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "log must be a %d-byte aligned device buffer", QMBX_ALIGN);
+    }
+    const LogLayout L = log_layout(n_i, n_j, cap);
+    if (log_bytes < L.total) return fail(QMBX_ERR_ARGUMENT, "log buffer smaller than its layout");
+    if (n_i > 0 && out64 == nullptr && out32 == nullptr) return fail(QMBX_ERR_ARGUMENT, "no output given");
+    if (n_j > 0 && g == nullptr) return fail(QMBX_ERR_ARGUMENT, "g_j must not be NULL");
+    const char* b = static_cast<const char*>(log);
+    LogHead head{};
+    QMBX_CUDA_TRY(cudaMemcpyAsync(&head, b, sizeof(head), cudaMemcpyDeviceToHost, s));
+    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
+    if (head.magic != kLogMagic || head.dir < 0 || head.dir > 2) {
+        return fail(QMBX_ERR_ARGUMENT, "the buffer holds no hit log (no logged forward call wrote it)");
+    }
+    if (head.n_i != n_i || head.n_j != n_j || head.cap != cap) {
+        return fail(QMBX_ERR_ARGUMENT, "the log was written for %lld x %lld rows and %lld hits, not %lld x %lld and %lld",
+                    (long long)head.n_i, (long long)head.n_j, (long long)head.cap, (long long)n_i, (long long)n_j,
+                    (long long)cap);
+    }
+    if (hits_needed) *hits_needed = (int64_t)head.count;
+    if ((int64_t)head.count > cap) {
+        return fail(QMBX_ERR_WORKSPACE, "the log holds %lld of the forward's %llu hits", (long long)cap, head.count);
+    }
+    if (n_i == 0) return QMBX_OK;
+    if (head.dir == 2 || n_j == 0) {
+        if (out64) QMBX_CUDA_TRY(cudaMemsetAsync(out64, 0, (size_t)n_i * sizeof(double2), s));
+        if (out32) QMBX_CUDA_TRY(cudaMemsetAsync(out32, 0, (size_t)n_i * sizeof(float2), s));
+        return QMBX_OK;
+    }
+    double2* res = reinterpret_cast<double2*>(const_cast<char*>(b) + L.res);
+    const int* dir = reinterpret_cast<const int*>(b + L.dir);
+    QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_i * sizeof(double2), s));
+    const PartView fwd = part_view(table_host, table_dev, QMBX_PART_FWD);
+    const PartView adj = part_view(table_host, table_dev, QMBX_PART_ADJ);
+    const int64_t nh = (int64_t)head.count;
+    const int64_t nw = n_i > n_j ? n_i : n_j;
+    const int4* hits = reinterpret_cast<const int4*>(b + L.hits);
+    const int2* drows = reinterpret_cast<const int2*>(b + L.diag_rows);
+    const double2* dvals = reinterpret_cast<const double2*>(b + L.diag_val);
+    if (f32) {
+        if (nh > 0) QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<true><<<grid_for(nh, kThreads), kThreads, 0, s>>>(hits, nh, dir, fwd, adj, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<true><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, dir, g, res));
+    } else {
+        if (nh > 0) QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<false><<<grid_for(nh, kThreads), kThreads, 0, s>>>(hits, nh, dir, fwd, adj, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<false><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, dir, g, res));
+    }
+    QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_i, kThreads), kThreads, 0, s>>>(res, reinterpret_cast<const int32_t*>(b + L.first), n_i, 1, out64, out32));
+    QMBX_LAUNCH_CHECK("adjoint from log");
+    return QMBX_OK;
+}
+
+}  // namespace
+}  // namespace qmbx
+
+extern "C" int qmbx_hitlog_bytes(int64_t n_i, int64_t n_j, int64_t cap, uint64_t* bytes) {
+    clear_error();
+    if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
+    if (n_i < 0 || n_j < 0 || cap < 0) return fail(QMBX_ERR_ARGUMENT, "sizes must not be negative");
+    *bytes = log_layout(n_i, n_j, cap).total;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_apply_within_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                        const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                                        int32_t same_configs, double* psi_j, void* workspace, uint64_t workspace_bytes,
+                                        void* log, uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream) {
+    clear_error();
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F64,
+                psi_i, reinterpret_cast<double2*>(psi_j), nullptr, 1, {}, nullptr, nullptr, 0};
+    int st = attach_log(a, log, log_bytes, log_cap);
+    if (st != QMBX_OK) return st;
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_f32c_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
+                                             const float* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
+                                             int32_t same_configs, int32_t include_diagonal, double* out_f64,
+                                             float* out_f32, void* workspace, uint64_t workspace_bytes, void* log,
+                                             uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream) {
+    clear_error();
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F32C,
+                psi_i, reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), include_diagonal,
+                {}, nullptr, nullptr, 0};
+    int st = attach_log(a, log, log_bytes, log_cap);
+    if (st != QMBX_OK) return st;
+    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_adjoint_logged(const void* table_host, const void* table_dev, const void* log,
+                                                uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
+                                                const double* g_j, double* out_i, int64_t* hits_needed,
+                                                qmbx_stream_t stream) {
+    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, false, g_j,
+                            reinterpret_cast<double2*>(out_i), nullptr, hits_needed,
+                            reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int qmbx_apply_within_adjoint_f32c_logged(const void* table_host, const void* table_dev, const void* log,
+                                                     uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
+                                                     const float* g_j, double* out_f64, float* out_f32,
+                                                     int64_t* hits_needed, qmbx_stream_t stream) {
+    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, true, g_j,
+                            reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), hits_needed,
+                            reinterpret_cast<cudaStream_t>(stream));
 }

@@ -356,8 +356,48 @@ __device__ __forceinline__ void test_tile(const TermTile<W>& tile, int count, co
     }
 }
 
+// What a forward walk of apply_within found, kept so that the adjoint
+// product on the same rows needs no second walk (qmbx_*_logged): one record
+// per (term, walked row) pair whose image was found among the looked-up
+// rows, and per walked row the summed diagonal coefficient.  hits == NULL:
+// nothing is recorded.
+struct HitLog {
+    int4* hits;                  // (walked first row, looked-up row, slot | parity << 31, 0)
+    unsigned long long* count;   // records found (more than cap: the log is incomplete)
+    int64_t cap;
+    int2* diag_rows;             // per walk index: (walked first row, looked-up row or -1)
+    double2* diag_val;           // per walk index: summed diagonal coefficient (sign folded)
+};
+
+// Record n (<= 32) queued hits (int2: slot | parity << 31, looked-up row) of
+// the walked row; every lane of the warp calls it.
+__device__ __forceinline__ void log_hits(const HitLog& log, int walked, const int2* q, int n, int lane) {
+    if (log.hits == nullptr || n <= 0) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(log.count, (unsigned long long)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (lane < n && base + lane < (unsigned long long)log.cap) {
+        const int2 h = q[lane];
+        log.hits[base + lane] = make_int4(walked, h.y, h.x, 0);
+    }
+}
+
+// One hit recorded by one thread (walks without hit queues).
+__device__ __forceinline__ void log_hit(const HitLog& log, int walked, int2 h) {
+    if (log.hits == nullptr) return;
+    const unsigned long long at = atomicAdd(log.count, 1ull);
+    if (at < (unsigned long long)log.cap) log.hits[at] = make_int4(walked, h.y, h.x, 0);
+}
+
+// The walked row's diagonal record (walk index u).
+__device__ __forceinline__ void log_diag(const HitLog& log, int64_t u, int walked, int64_t pos, double re, double im) {
+    if (log.hits == nullptr) return;
+    log.diag_rows[u] = make_int2(walked, (int)pos);
+    log.diag_val[u] = make_double2(re, im);
+}
+
 // Defaults for the optional parts of the visitor protocol: no shared memory,
-// no per-block set-up or flush.
+// no per-block set-up or flush, no hit log.
 struct VisitorBase {
     template <class Acc, class K>
     __device__ __forceinline__ void flush(Acc&, int64_t, const K&) const {}
@@ -368,6 +408,14 @@ struct VisitorBase {
     __device__ __forceinline__ void apply_hit(Acc&, int2) const {}
     __device__ __forceinline__ void block_init(int*) const {}
     __device__ __forceinline__ void block_flush(int*) const {}
+    // hit-queue drains: record the n hits about to be applied (all lanes call)
+    template <class Acc>
+    __device__ __forceinline__ void record_hits(const Acc&, const int2*, int, int) const {}
+    // one hit applied at once by one lane (serial group walks)
+    template <class Acc>
+    __device__ __forceinline__ void record_hit(const Acc&, int2) const {}
+    // pivot hit-queue drains: the same for (slot | parity << 31, looked-up row, walk index) hits
+    __device__ __forceinline__ void record_row_hits(const int4*, int, int) const {}
 };
 
 // Visitor protocol:
@@ -504,6 +552,7 @@ struct HitQueue {
 
 template <class V>
 __device__ __forceinline__ void queue_drain(const V& v, typename V::Acc& acc, HitQueue& hq, int lane, bool all) {
+    v.record_hits(acc, hq.q, all ? hq.count : 32, lane);
     if (all) {
         if (lane < hq.count) v.apply_hit(acc, hq.q[lane]);
         __syncwarp();
@@ -638,7 +687,10 @@ __device__ __forceinline__ void walk_group_serial(const V& v, typename V::Acc& a
     const int2 se = __ldg(pv.groups + g);
     for (int64_t t = se.x; t < se.y; ++t) {
         int2 h;
-        if (test_term<W, DIAG>(v, acc, c, pv, t, h)) v.apply_hit(acc, h);
+        if (test_term<W, DIAG>(v, acc, c, pv, t, h)) {
+            v.record_hit(acc, h);
+            v.apply_hit(acc, h);
+        }
     }
 }
 
@@ -891,6 +943,7 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
                                 hcount += __popc(m);
                                 __syncwarp();
                                 if (hcount >= 32) {
+                                    v.record_row_hits(hq, 32, lane);
                                     v.apply_row_hit(hq[lane]);
                                     __syncwarp();
                                     if (lane < hcount - 32) hq[lane] = hq[32 + lane];
@@ -910,6 +963,7 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
         __syncthreads();
     }
     if constexpr (V::kStateless) {
+        v.record_row_hits(hq, hcount, lane);
         if (lane < hcount) v.apply_row_hit(hq[lane]);
     }
     __syncthreads();

@@ -182,6 +182,50 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(int64_t n, const int64_t
     }
 }
 
+// y = A x for rows with few entries (the mean below kFewEntries): one thread
+// per row, entries summed in order.
+__global__ void __launch_bounds__(kThreads) spmv_rows_kernel(int64_t n, const int64_t* __restrict__ row_ptr,
+                                                             const int32_t* __restrict__ col,
+                                                             const double2* __restrict__ val,
+                                                             const double2* __restrict__ x, double2* __restrict__ y) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int64_t b = __ldg(row_ptr + j), e = __ldg(row_ptr + j + 1);
+    double re = 0.0, im = 0.0;
+    for (int64_t k = b; k < e; ++k) {
+        const double2 v = __ldg(val + k);
+        const double2 p = __ldg(x + __ldg(col + k));
+        re += v.x * p.x - v.y * p.y;
+        im += v.x * p.y + v.y * p.x;
+    }
+    y[j] = make_double2(re, im);
+}
+constexpr int64_t kFewEntries = 4;
+
+// Y = A X for m vectors (X, Y row-major [n][m]): one warp per row, lane l
+// owns vectors l, l + 32, ...; the row's entries are read once per 32
+// vectors (the same address across lanes) and summed in order.
+__global__ void __launch_bounds__(kThreads) spmm_kernel(int64_t n, int m, const int64_t* __restrict__ row_ptr,
+                                                        const int32_t* __restrict__ col,
+                                                        const double2* __restrict__ val,
+                                                        const double2* __restrict__ x, double2* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t j = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); j < n; j += warps) {
+        const int64_t b = __ldg(row_ptr + j), e = __ldg(row_ptr + j + 1);
+        for (int c = lane; c < m; c += 32) {
+            double re = 0.0, im = 0.0;
+            for (int64_t k = b; k < e; ++k) {
+                const double2 v = __ldg(val + k);
+                const double2 p = __ldg(x + (int64_t)__ldg(col + k) * m + c);
+                re += v.x * p.x - v.y * p.y;
+                im += v.x * p.y + v.y * p.x;
+            }
+            y[j * m + c] = make_double2(re, im);
+        }
+    }
+}
+
 struct MatrixLayout {
     HashRows rows;
     int32_t* count;
@@ -373,5 +417,29 @@ extern "C" int qmbx_matrix_apply(int64_t n, const int64_t* row_ptr, const int32_
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     QMBX_KERNEL(kGroupSpmv, s, spmv_kernel<<<grouped_grid(n), kThreads, 0, s>>>(n, row_ptr, col, reinterpret_cast<const double2*>(val), reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(y)));
     QMBX_LAUNCH_CHECK("spmv_kernel");
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_matrix_apply_many(int64_t n, int64_t nnz, int32_t m, const int64_t* row_ptr, const int32_t* col,
+                                      const double* val, const double* x, double* y, qmbx_stream_t stream) {
+    clear_error();
+    if (n < 0 || n >= (int64_t(1) << 31)) return fail(QMBX_ERR_ARGUMENT, "row count out of range");
+    if (nnz < 0 || m < 1) return fail(QMBX_ERR_ARGUMENT, "entry count or vector count out of range");
+    if (n == 0) return QMBX_OK;
+    if (row_ptr == nullptr || col == nullptr || (nnz > 0 && val == nullptr) || x == nullptr || y == nullptr) {
+        return fail(QMBX_ERR_ARGUMENT, "pointers must not be NULL");
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const double2* v = reinterpret_cast<const double2*>(val);
+    const double2* xx = reinterpret_cast<const double2*>(x);
+    double2* yy = reinterpret_cast<double2*>(y);
+    if (m > 1) {
+        QMBX_KERNEL(kGroupSpmv, s, spmm_kernel<<<grouped_grid(n), kThreads, 0, s>>>(n, m, row_ptr, col, v, xx, yy));
+    } else if (nnz < kFewEntries * n) {
+        QMBX_KERNEL(kGroupSpmv, s, spmv_rows_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, row_ptr, col, v, xx, yy));
+    } else {
+        QMBX_KERNEL(kGroupSpmv, s, spmv_kernel<<<grouped_grid(n), kThreads, 0, s>>>(n, row_ptr, col, v, xx, yy));
+    }
+    QMBX_LAUNCH_CHECK("matrix product");
     return QMBX_OK;
 }

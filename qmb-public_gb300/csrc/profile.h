@@ -8,7 +8,7 @@ namespace qmbx {
 // kGroupEnumerate is the main term walk; kGroupDiagonal the separate
 // passes over diagonal terms that follow it; kGroupSort the radix sorts
 // (histogram, scan and scatter passes); kGroupSpmv the products with a
-// materialised matrix
+// materialised matrix and the adjoint products replayed from a hit log
 enum ProfileGroup {
     kGroupEnumerate = 0,
     kGroupKeys = 1,

@@ -162,6 +162,7 @@ class Hamiltonian:
             case _:
                 raise ValueError(f"Unknown kind: {kind}")
         self._tables: dict = {}
+        self._log_caps: dict = {}
         # where compiled term tables are cached across processes (compile_table); QMBX_TABLE_CACHE by default
         self.table_cache = table_cache if table_cache is not None else os.environ.get("QMBX_TABLE_CACHE")
 
@@ -213,9 +214,26 @@ class Hamiltonian:
 
     # -- apply_within ---------------------------------------------------------
 
+    # hit records a logged forward call may keep (16 bytes each): a first guess, then what the
+    # last call on rows of the same shape needed
+    _LOG_FIRST_GUESS = 1 << 22
+    # differentiable apply_within records the forward walk's hits for its backward; False: the
+    # backward walks the terms again with the adjoint kernel
+    hit_log = True
+
+    def _log_capacity(self, n_i: int, n_j: int, device: torch.device) -> int:
+        cap = self._log_caps.get((device.index, n_i, n_j), self._LOG_FIRST_GUESS)
+        free, _ = torch.cuda.mem_get_info(device)
+        return int(min(cap, free // 8 // 16))
+
     def _apply(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor, *, adjoint: bool,
-               out_dtype: torch.dtype | None = None, include_diagonal: bool = True) -> torch.Tensor:
-        """Forward (psi_i on configs_i -> configs_j) or adjoint (g on configs_j -> configs_i) application."""
+               out_dtype: torch.dtype | None = None, include_diagonal: bool = True, log: bool = False):
+        """Forward (psi_i on configs_i -> configs_j) or adjoint (g on configs_j -> configs_i) application.
+
+        With ``log`` (forward only) the walk also records its hits and the
+        result is ``(out, record)``; ``_adjoint_from_log(record, g)`` then gives
+        the adjoint product on the same rows without walking the terms again.
+        """
         device = configs_i.device
         configs_i = self._configs(configs_i, "configs_i")
         configs_j = self._configs(configs_j, "configs_j", device)
@@ -233,17 +251,27 @@ class Hamiltonian:
         with torch.cuda.device(device):
             ws = _workspace(need.value, device)
             stream = _stream(device)
+            record = None
+            log_args = ()
+            if log and not adjoint:
+                cap = self._log_capacity(n_i, n_j, device)
+                nbytes = ctypes.c_uint64(0)
+                _native.check(lib.qmbx_hitlog_bytes(n_i, n_j, cap, ctypes.byref(nbytes)))
+                buf = _workspace(nbytes.value, device)
+                record = _HitRecord(table, buf, cap, n_i, n_j, psi.dtype, include_diagonal)
+                log_args = (buf.data_ptr(), buf.numel(), cap)
             if psi.dtype == torch.complex128:
                 out = torch.empty(n_out, dtype=torch.complex128, device=device)
-                name = "qmbx_apply_within_adjoint" if adjoint else "qmbx_apply_within"
                 if adjoint:
-                    args = (table.h, table.d, configs_i.data_ptr(), n_i, configs_j.data_ptr(), psi.data_ptr(), n_j,
-                            same, out.data_ptr(), ws.data_ptr(), ws.numel(), stream)
+                    _native.call("qmbx_apply_within_adjoint", table.h, table.d, configs_i.data_ptr(), n_i,
+                                 configs_j.data_ptr(), psi.data_ptr(), n_j, same, out.data_ptr(), ws.data_ptr(),
+                                 ws.numel(), stream)
                 else:
-                    args = (table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j,
-                            same, out.data_ptr(), ws.data_ptr(), ws.numel(), stream)
-                _native.call(name, *args)
-                return out if out_dtype in (None, torch.complex128) else out.to(out_dtype)
+                    _native.call("qmbx_apply_within_logged" if record else "qmbx_apply_within", table.h, table.d,
+                                 configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j, same,
+                                 out.data_ptr(), ws.data_ptr(), ws.numel(), *log_args, stream)
+                out = out if out_dtype in (None, torch.complex128) else out.to(out_dtype)
+                return (out, record) if log and not adjoint else out
             want64 = out_dtype == torch.complex128
             out = torch.empty(n_out, dtype=torch.complex128 if want64 else torch.complex64, device=device)
             o64, o32 = (out.data_ptr(), None) if want64 else (None, out.data_ptr())
@@ -252,10 +280,45 @@ class Hamiltonian:
                              configs_j.data_ptr(), psi.data_ptr(), n_j, same, int(include_diagonal), o64, o32,
                              ws.data_ptr(), ws.numel(), stream)
             else:
-                _native.call("qmbx_apply_within_f32c", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i,
-                             configs_j.data_ptr(), n_j, same, int(include_diagonal), o64, o32, ws.data_ptr(),
-                             ws.numel(), stream)
-            return out
+                _native.call("qmbx_apply_within_f32c_logged" if record else "qmbx_apply_within_f32c", table.h,
+                             table.d, configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j, same,
+                             int(include_diagonal), o64, o32, ws.data_ptr(), ws.numel(), *log_args, stream)
+            return (out, record) if log and not adjoint else out
+
+    def _adjoint_from_log(self, record: "_HitRecord", g: torch.Tensor,
+                          out_dtype: torch.dtype | None = None) -> torch.Tensor | None:
+        """The adjoint product of a logged forward call for g on its output rows, or None when the
+        record is incomplete (the capacity for rows of this shape is raised for the next call)."""
+        device = record.buf.device
+        g = g.to(record.dtype).contiguous()
+        if g.shape != (record.n_j,):
+            raise RuntimeError(f"g must have shape [{record.n_j}].")
+        needed = ctypes.c_int64(0)
+        lib = _native.library()
+        table = record.table
+        with torch.cuda.device(device):
+            stream = _stream(device)
+            if record.dtype == torch.complex128:
+                out = torch.empty(record.n_i, dtype=torch.complex128, device=device)
+                status = lib.qmbx_apply_within_adjoint_logged(table.h, table.d, record.buf.data_ptr(),
+                                                              record.buf.numel(), record.cap, record.n_i, record.n_j,
+                                                              g.data_ptr(), out.data_ptr(), ctypes.byref(needed),
+                                                              stream)
+            else:
+                want64 = out_dtype == torch.complex128
+                out = torch.empty(record.n_i, dtype=torch.complex128 if want64 else torch.complex64, device=device)
+                o64, o32 = (out.data_ptr(), None) if want64 else (None, out.data_ptr())
+                status = lib.qmbx_apply_within_adjoint_f32c_logged(table.h, table.d, record.buf.data_ptr(),
+                                                                   record.buf.numel(), record.cap, record.n_i,
+                                                                   record.n_j, g.data_ptr(), o64, o32,
+                                                                   ctypes.byref(needed), stream)
+        key = (device.index, record.n_i, record.n_j)
+        if status == _native.QMBX_ERR_WORKSPACE:
+            self._log_caps[key] = int(needed.value * 1.25) + 1024
+            return None
+        _native.check(status)
+        self._log_caps[key] = int(needed.value * 1.25) + 1024
+        return out
 
     def apply_within(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor) -> torch.Tensor:
         """H psi restricted to configs_j (qmb/hamiltonian.py:104-131); differentiable in psi_i.
@@ -452,15 +515,18 @@ class HamiltonianMatrix:
         self.nnz = col.shape[0]
 
     def apply(self, x: torch.Tensor) -> torch.Tensor:
-        """A x for complex128 x on the matrix's rows (bit-identical on every call)."""
-        if x.dtype != torch.complex128 or x.dim() != 1 or x.shape[0] != self.n:
-            raise RuntimeError(f"x must be complex128 of shape [{self.n}].")
+        """A x for complex128 x of shape [n], or of shape [n, m] (m vectors, one pass over the matrix);
+        bit-identical on every call."""
+        if x.dtype != torch.complex128 or x.dim() not in (1, 2) or x.shape[0] != self.n or \
+                (x.dim() == 2 and x.shape[1] < 1):
+            raise RuntimeError(f"x must be complex128 of shape [{self.n}] or [{self.n}, m].")
         if x.device != self.val.device:
             raise RuntimeError("x must be on the matrix's device.")
         x = x.contiguous()
         y = torch.empty_like(x)
+        m = 1 if x.dim() == 1 else x.shape[1]
         with torch.cuda.device(x.device):
-            _native.call("qmbx_matrix_apply", self.n, self.row_ptr.data_ptr(), self.col.data_ptr(),
+            _native.call("qmbx_matrix_apply_many", self.n, self.nnz, m, self.row_ptr.data_ptr(), self.col.data_ptr(),
                          self.val.data_ptr(), x.data_ptr(), y.data_ptr(), _stream(x.device))
         return y
 
@@ -473,15 +539,36 @@ class HamiltonianMatrix:
         return dense
 
 
+class _HitRecord:
+    """What a logged forward apply_within found (a device buffer), for its adjoint product."""
+
+    def __init__(self, table: _Table, buf: torch.Tensor, cap: int, n_i: int, n_j: int, dtype: torch.dtype,
+                 include_diagonal: bool):
+        self.table, self.buf, self.cap, self.n_i, self.n_j = table, buf, cap, n_i, n_j
+        self.dtype, self.include_diagonal = dtype, include_diagonal
+
+
 class _ApplyWithin(torch.autograd.Function):
-    """y = H psi restricted to configs_j; backward applies H^dagger (the adjoint kernel)."""
+    """y = H psi restricted to configs_j; backward applies H^dagger.
+
+    The forward walk records its hits, and the backward replays that record
+    (the adjoint needs exactly the (term, row) pairs the forward found); when
+    the record could not hold them all, the backward walks the terms with
+    the adjoint kernel instead.
+    """
 
     @staticmethod
     def forward(ctx, ham: Hamiltonian, configs_i, psi_i, configs_j, out_dtype):
         ctx.ham = ham
         ctx.in_dtype = psi_i.dtype
         ctx.save_for_backward(configs_i, configs_j)
-        return ham._apply(configs_i, psi_i.detach(), configs_j, adjoint=False, out_dtype=out_dtype)
+        deterministic = os.environ.get("QMBX_DETERMINISTIC", "")[:1] not in ("", "0")
+        if not ham.hit_log or deterministic:  # the replay adds with atomics; the walk can be fixed-order
+            ctx.record = None
+            return ham._apply(configs_i, psi_i.detach(), configs_j, adjoint=False, out_dtype=out_dtype)
+        out, ctx.record = ham._apply(configs_i, psi_i.detach(), configs_j, adjoint=False, out_dtype=out_dtype,
+                                     log=True)
+        return out
 
     @staticmethod
     def backward(ctx, grad):
@@ -489,6 +576,9 @@ class _ApplyWithin(torch.autograd.Function):
         if grad is None:
             return None, None, None, None, None
         g = grad.to(ctx.in_dtype).contiguous()
-        gi = ctx.ham._apply(configs_i, g, configs_j, adjoint=True,
-                            out_dtype=torch.complex128 if ctx.in_dtype == torch.complex128 else None)
+        want = torch.complex128 if ctx.in_dtype == torch.complex128 else None
+        gi = ctx.ham._adjoint_from_log(ctx.record, g, want) if ctx.record is not None else None
+        if gi is None:
+            gi = ctx.ham._apply(configs_i, g, configs_j, adjoint=True, out_dtype=want)
+        ctx.record = None
         return None, None, gi.to(ctx.in_dtype), None, None

@@ -45,6 +45,15 @@ def test_committed_profile_figures_are_keyed_to_the_kernel_sources(tmp_path, mon
     assert bench.ncu_figures("fresh")["warp_instructions_per_launch"] == 5e8
     assert bench.ncu_figures("stale") is None
     assert bench.ncu_figures("absent") is None
+    # a figure that names its kernel's sources is keyed to those alone
+    (prof / "apply.json").write_text(json.dumps({"kernel_sources_sha": bench.kernel_sources_sha(bench.APPLY_SOURCES),
+                                                 "sources": list(bench.APPLY_SOURCES)}))
+    assert bench.ncu_figures("apply") is not None
+    (tmp_path / "qmb-public_gb300/csrc/relative.cu").write_bytes(b"// changed")
+    assert bench.ncu_figures("apply") is not None
+    assert bench.ncu_figures("fresh") is None
+    (tmp_path / "qmb-public_gb300/csrc/apply.cu").write_bytes(b"// changed")
+    assert bench.ncu_figures("apply") is None
 
 
 def test_committed_profile_json_files_parse():

@@ -145,15 +145,17 @@ def _mlp(c3, device):
     return bench._Mlp(8 * c3["nq"], device, seed=c3["seed"])
 
 
-def _engine_walks(fn) -> int:
-    """Term-walk launches made by fn (the forward walk plus, when taken, the adjoint walk)."""
+def _engine_walks(fn, replays: bool = False):
+    """Term-walk launches made by fn (the forward walk plus, when taken, the adjoint walk); with
+    ``replays`` also the launches that replay a hit log or apply a stored matrix."""
     native = importlib.import_module("qmb-public_gb300._native")
     native.profile_enable(True)
     fn()
     torch.cuda.synchronize()
     prof = native.profile_read()
     native.profile_enable(False)
-    return prof["groups"]["enumerate"][0]
+    walks = prof["groups"]["enumerate"][0]
+    return (walks, prof["groups"]["spmv"][0]) if replays else walks
 
 
 @pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
@@ -180,10 +182,21 @@ def test_c3_gradient_through_adjoint_matches_dense(c3_subset, dtype, cuda_device
 
     e_dense, g_dense = grads("dense")
     holder = {}
-    walks = _engine_walks(lambda: holder.setdefault("adj", grads("adjoint")))
+    # the backward through the adjoint kernel: the forward walk and the adjoint walk both run
+    ham.hit_log = False
+    try:
+        walks = _engine_walks(lambda: holder.setdefault("adj", grads("adjoint")))
+    finally:
+        ham.hit_log = True
     e_adj, g_adj = holder["adj"]
-    # the forward walk and the adjoint walk both ran (the shortcut takes one)
     assert walks == 2
+    # the backward from the forward walk's hit log: one walk, then the replay (a first call on
+    # rows of this shape may find the log too small and walk; the second one fits)
+    grads("adjoint")
+    walks, replays = _engine_walks(lambda: holder.setdefault("log", grads("adjoint")), replays=True)
+    assert walks == 1 and replays >= 1
+    e_log, g_log = holder["log"]
+    # the Hermitian shortcut: the forward walk only
     assert _engine_walks(lambda: holder.setdefault("cut", grads("shortcut"))) == 1
     e_cut, g_cut = holder["cut"]
     if dtype == torch.complex128:
@@ -193,13 +206,15 @@ def test_c3_gradient_through_adjoint_matches_dense(c3_subset, dtype, cuda_device
         # 1e-7 Ha of FP64 (the path's stated bound), gradients to FP32 rounding
         e_tol, rtol = 1e-7, 1e-4
     assert abs(e_adj - e_dense) <= e_tol
+    assert abs(e_log - e_dense) <= e_tol
     assert abs(e_cut - e_dense) <= e_tol
     # elementwise to rtol, with an absolute floor of rtol times the largest
     # gradient entry: some entries vanish exactly in FP64 (the log-amplitude
     # bias: E does not change when psi is scaled) and carry FP32 rounding here
     atol = rtol * max(b.abs().max().item() for b in g_dense)
-    for a, b, cut in zip(g_adj, g_dense, g_cut):
+    for a, b, lg, cut in zip(g_adj, g_dense, g_log, g_cut):
         assert torch.allclose(a, b, rtol=rtol, atol=atol)
+        assert torch.allclose(lg, b, rtol=rtol, atol=atol)
         assert torch.allclose(cut, b, rtol=rtol, atol=atol)
 
 

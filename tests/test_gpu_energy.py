@@ -2,7 +2,7 @@
 
 E(psi) = Re<psi|H|psi> / <psi|psi> with H psi from apply_within (FP64 or the
 FP32-compensated path) and the backward pass through the hand-written
-adjoint.  Checked against a dense FP64 H built by the CPU oracle (energy to
+adjoint (a replay of the forward walk's hits, or the adjoint walk).  Checked against a dense FP64 H built by the CPU oracle (energy to
 1e-12 relative, gradient to 1e-10 relative), against central finite
 differences (1e-6 relative), and, through a small MLP wave function, against
 the same network evaluated with the dense matrix in torch.
@@ -37,9 +37,13 @@ def _dense_energy_and_grad(h, psi):
     return e, grad
 
 
+@pytest.mark.parametrize("hit_log", [True, False])
 @pytest.mark.parametrize("case", ["ab_initio_10_complex", "ab_initio_6", "random_terms_fermi"])
-def test_energy_and_gradient_match_dense_fp64(case, cuda_device):
+def test_energy_and_gradient_match_dense_fp64(case, hit_log, cuda_device):
+    """Non-Hermitian operators (random_terms_fermi) take the backward of apply_within: from the
+    forward walk's hit log, or (hit_log False) from the adjoint kernel's walk."""
     g, rows, h, ham = _setup(case)
+    ham.hit_log = hit_log
     rng = np.random.default_rng(1)
     psi0 = rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])
     c = torch.from_numpy(rows).to(cuda_device)

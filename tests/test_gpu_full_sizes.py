@@ -154,3 +154,23 @@ def test_find_relative_with_sampled_threshold(k, cuda_device):
     want, _ = oracle.find_relative(site, kind, coef, rows, psi, k, rows, 1, rule="ranked")
     got = ham.find_relative(torch.from_numpy(rows).to(cuda_device), torch.from_numpy(psi).to(cuda_device), k).cpu().numpy()
     assert np.array_equal(got, want)
+
+
+def test_find_relative_when_the_sample_misleads(cuda_device):
+    # pass 1 counts every 16th source row; give exactly those rows large amplitudes, so the
+    # sample predicts 16 times the records above any weight and puts the threshold too high:
+    # the emission pass then keeps fewer than k records, and an unsampled histogram pass and a
+    # second emission pass take over (four walks in all)
+    qmb = __import__("qmb_gb300")
+    native = __import__("importlib").import_module("qmb-public_gb300._native")
+    site, kind, coef = (x.numpy() for x in qmb.terms.integral_hamiltonian_tables(9, seed=3))
+    rows = qmb.terms.random_determinants(9, 4, 4, 6000, seed=8)
+    rng = np.random.default_rng(11)
+    psi = (rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])) * 1e-3
+    psi[::16] *= 1e6
+    ham = Hamiltonian((torch.from_numpy(site), torch.from_numpy(kind), torch.from_numpy(coef)), kind="fermi")
+    k = 100000
+    want, _ = oracle.find_relative(site, kind, coef, rows, psi, k, rows, 1, rule="ranked")
+    got = ham.find_relative(torch.from_numpy(rows).to(cuda_device), torch.from_numpy(psi).to(cuda_device), k).cpu().numpy()
+    assert native.find_relative_stats()["walks"] == 4
+    assert np.array_equal(got, want)

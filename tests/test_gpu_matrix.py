@@ -79,3 +79,31 @@ def test_matrix_rejects_repeated_rows(cuda_device):
     rows = torch.from_numpy(np.concatenate([g["configs_i"], g["configs_i"][:3]])).to(cuda_device)
     with pytest.raises(RuntimeError, match="distinct"):
         _ham(g).matrix(rows)
+
+
+@pytest.mark.parametrize("n_rows", [300, 6000])
+def test_matrix_products_one_and_many_vectors(n_rows, cuda_device):
+    # a sparse basis (random determinants, a few entries per row: a thread per row) and a denser one
+    # (a warp per row); m vectors in one pass equal m single products, to 1e-12 of the absolute sums
+    qmb = __import__("qmb_gb300")
+    site, kind, coef = (x.numpy() for x in qmb.terms.integral_hamiltonian_tables(12, seed=5))
+    rows = qmb.terms.random_determinants(12, 4, 4, n_rows, seed=6)
+    ham = Hamiltonian((torch.from_numpy(site), torch.from_numpy(kind), torch.from_numpy(coef)), kind="fermi")
+    drows = torch.from_numpy(rows).to(cuda_device)
+    mat = ham.matrix(drows)
+    assert (mat.nnz < 4 * rows.shape[0]) == (n_rows == 300)  # which product kernel runs
+    gen = torch.Generator(device=cuda_device).manual_seed(7)
+    x = torch.randn((rows.shape[0], 3), dtype=torch.complex128, device=cuda_device, generator=gen)
+    mag = np.zeros_like(coef)
+    mag[:, 0] = np.hypot(coef[:, 0], coef[:, 1])
+    many = mat.apply(x)
+    assert torch.equal(torch.view_as_real(many), torch.view_as_real(mat.apply(x)))
+    for c in range(3):
+        col = x[:, c].contiguous()
+        one = mat.apply(col)
+        assert torch.equal(torch.view_as_real(one), torch.view_as_real(mat.apply(col)))
+        ref = ham.apply_within(drows, col, drows)
+        scale = np.abs(oracle.apply_within(site, kind, mag, rows, np.abs(col.cpu().numpy()).astype(np.complex128),
+                                           rows, 2))
+        assert np.all(np.abs((one - ref).cpu().numpy()) <= 1e-12 * scale + 1e-300)
+        assert np.all(np.abs((many[:, c] - ref).cpu().numpy()) <= 1e-12 * scale + 1e-300)
