@@ -582,6 +582,11 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
     native.profile_enable(False)
     n_enum, ms_enum = prof["groups"]["enumerate"]
     walks_per_step = n_enum / args.steps
+    n_replay, ms_replay = prof["groups"]["spmv"]
+    # hits of one forward walk (the records the backward replays)
+    y_rec, record = ham._apply(ci, psi32, cj, adjoint=False, log=True)
+    ham._adjoint_from_log(record, y_rec)
+    hits = record.hits or 0
 
     if rank != 0:
         return None
@@ -634,6 +639,13 @@ def run_ours(args, wl, rank: int, world: int) -> dict | None:
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "hit_log": {"hits_per_step": hits, "record_bytes_per_step": 16 * hits,
+                    # per hit: its 16-byte record, the FP32 hi/lo coefficient (16) and g (8) it gathers;
+                    # per configs_i row: the result (16, FP64 atomics) and its first row (4)
+                    # (both replay kernels of a step timed together)
+                    "replay_roofline": hbm_roofline(hits * 40 + n_i * 20, ms_replay / args.steps,
+                                                    "hit-log replay (log_adjoint_kernel + diagonal records)",
+                                                    launches_per_step=n_replay / args.steps)},
         "walked_pairs_per_s": {"value": world * walks_per_step * T * n_i / (ms_step32 * 1e-3),
                                "walks_per_step": walks_per_step,
                                "what": "(term, row) pairs the term walks visit: each walk covers configs_i's "

@@ -213,43 +213,47 @@ int qmbx_matrix_apply_many(int64_t n, int64_t nnz, int32_t m, const int64_t* row
  * also records what its walk found, and the adjoint product on the same rows
  * computed from that record without a second walk -- the backward of an
  * energy gradient needs exactly the (term, row) pairs the forward found.
+ *
  * qmbx_hitlog_bytes sizes the caller's log buffer (device, 256-byte aligned)
- * for n_i x n_j rows and log_cap hit records (16 bytes each).  The _logged
- * forwards take the same arguments as qmbx_apply_within /
- * qmbx_apply_within_f32c plus the log; the _logged adjoints take the log,
- * the same table and row counts, and g_j, and give what
- * qmbx_apply_within_adjoint(_f32c) gives (include_diagonal as in the
- * forward).  An adjoint call synchronises the stream to read the hit count;
- * when the forward found more hits than log_cap it returns
- * QMBX_ERR_WORKSPACE with the count in *hits_needed (a caller then runs
- * qmbx_apply_within_adjoint(_f32c), or a larger log next time).  The log's
- * header keeps the forward's n_i, n_j (n_i when same_configs was set) and
- * log_cap; an adjoint call with other values, or on a buffer no logged
- * forward wrote, returns QMBX_ERR_ARGUMENT before reading the records.  The
- * adjoint adds with FP64 atomics (not bitwise repeatable).
+ * for n_i x n_j rows and log_cap hit records (16 bytes each); the buffer also
+ * holds the forward's workspace, whose row sets the adjoint reuses, so the
+ * _logged forwards take no workspace.  They take the arguments of
+ * qmbx_apply_within / qmbx_apply_within_f32c plus the log.  The _logged
+ * adjoints take the log, the same table, row counts, same_configs and
+ * log_cap (and include_diagonal for the FP32 path) and g_j, and give what
+ * qmbx_apply_within_adjoint(_f32c) gives, without synchronising: a kernel
+ * reads the log's header on the device and either replays the record, or,
+ * when the forward found more than log_cap hits, walks the adjoint over the
+ * row sets the forward left in the buffer.  A buffer no logged forward wrote
+ * with these arguments gives NaN outputs.  qmbx_hitlog_count enqueues a copy
+ * of the forward's hit count to *count (host pinned or device memory), for
+ * sizing the next log.  The replay adds with FP64 atomics (not bitwise
+ * repeatable).  The log must stay allocated until the adjoint's work ends.
  * ------------------------------------------------------------------------- */
 
-int qmbx_hitlog_bytes(int64_t n_i, int64_t n_j, int64_t log_cap, uint64_t* bytes);
+int qmbx_hitlog_bytes(const void* table_host, int64_t n_i, int64_t n_j, int32_t same_configs, int64_t log_cap,
+                      uint64_t* bytes);
+
+int qmbx_hitlog_count(const void* log, unsigned long long* count, qmbx_stream_t stream);
 
 int qmbx_apply_within_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
                              const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
-                             int32_t same_configs, double* psi_j, void* workspace, uint64_t workspace_bytes, void* log,
-                             uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream);
+                             int32_t same_configs, double* psi_j, void* log, uint64_t log_bytes, int64_t log_cap,
+                             qmbx_stream_t stream);
 
 int qmbx_apply_within_f32c_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
                                   const float* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
                                   int32_t same_configs, int32_t include_diagonal, double* out_f64, float* out_f32,
-                                  void* workspace, uint64_t workspace_bytes, void* log, uint64_t log_bytes,
-                                  int64_t log_cap, qmbx_stream_t stream);
+                                  void* log, uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream);
 
 int qmbx_apply_within_adjoint_logged(const void* table_host, const void* table_dev, const void* log,
-                                     uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j, const double* g_j,
-                                     double* out_i, int64_t* hits_needed, qmbx_stream_t stream);
+                                     uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
+                                     int32_t same_configs, const double* g_j, double* out_i, qmbx_stream_t stream);
 
 int qmbx_apply_within_adjoint_f32c_logged(const void* table_host, const void* table_dev, const void* log,
                                           uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
-                                          const float* g_j, double* out_f64, float* out_f32, int64_t* hits_needed,
-                                          qmbx_stream_t stream);
+                                          int32_t same_configs, int32_t include_diagonal, const float* g_j,
+                                          double* out_f64, float* out_f32, qmbx_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * diagonal_term: out[c] = sum of s * coef_t over terms with t|c> = s|c>.
@@ -348,11 +352,17 @@ int qmbx_single_relative(const void* table_host, const void* table_dev, const ui
  * Optionally (both or neither) la, the rows' log amplitudes so far (double
  * [n]), and a_out (double [4][n]): each child's la + its normalised log
  * amplitude -- after the last site, the log amplitude the forward gives the
- * configuration, so psi needs only the phase network.
+ * configuration, so psi needs only the phase network.  Rows whose gp is not
+ * finite have no children (-inf).  Optionally bad (device int32, zeroed by
+ * the caller): children whose value is NaN or +inf are written as -FLT_MAX
+ * and counted, so a descending sort puts them after the finite values.
  * qmbx_sampler_take: the m chosen children (index int64 [m] into [4][n]):
  * occupations occ_out uint8 [m][sites] from occ_in, network inputs xf_out
  * float [m][2 sites] (sites up to `site` written), counts, lp, gp, and
- * (optionally, both or neither) la_out from a_in.
+ * (optionally, both or neither) la_out from a_in.  With bad (the site
+ * call's counter), chosen rows the reference's selection would drop get gp
+ * -inf: those written as -FLT_MAX, and those at places batch - *bad and
+ * beyond (the places its NaN / +inf values take at the top of its sort).
  * ------------------------------------------------------------------------- */
 
 int qmbx_sampler_log_amplitude(int64_t rows, int32_t sites, int32_t spin_up, int32_t spin_down, const float* deltas,
@@ -364,12 +374,12 @@ int qmbx_sampler_log_amplitude_grad(int64_t rows, int32_t sites, int32_t spin_up
 
 int qmbx_sampler_site(int64_t n, int32_t site, int32_t sites, int32_t spin_up, int32_t spin_down, const float* delta,
                       const int32_t* counts, const float* lp, const float* gp, const float* uniforms, float* l_out,
-                      float* t_out, const double* la, double* a_out, qmbx_stream_t stream);
+                      float* t_out, const double* la, double* a_out, int32_t* bad, qmbx_stream_t stream);
 
 int qmbx_sampler_take(int64_t m, int64_t n, int32_t site, int32_t sites, const int64_t* index, const uint8_t* occ_in,
                       const int32_t* counts_in, const float* l_in, const float* t_in, uint8_t* occ_out, float* xf_out,
                       int32_t* counts_out, float* lp_out, float* gp_out, const double* a_in, double* la_out,
-                      qmbx_stream_t stream);
+                      int64_t batch, const int32_t* bad, qmbx_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Tracing (no counterpart in the reference, which has none).

@@ -44,14 +44,14 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_apply_within_f32c": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
     "qmbx_apply_within_adjoint_f32c": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P]),
     "qmbx_diagonal_term": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P]),
-    "qmbx_hitlog_bytes": (ctypes.c_int, [_I64, _I64, _I64, _PU64]),
-    "qmbx_apply_within_logged": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P, _U64, _P, _U64, _I64,
-                                                _P]),
-    "qmbx_apply_within_f32c_logged": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _I32, _P, _P, _P, _U64, _P,
-                                                     _U64, _I64, _P]),
-    "qmbx_apply_within_adjoint_logged": (ctypes.c_int, [_P, _P, _P, _U64, _I64, _I64, _I64, _P, _P, _PI64, _P]),
-    "qmbx_apply_within_adjoint_f32c_logged": (ctypes.c_int, [_P, _P, _P, _U64, _I64, _I64, _I64, _P, _P, _P, _PI64,
-                                                             _P]),
+    "qmbx_hitlog_bytes": (ctypes.c_int, [_P, _I64, _I64, _I32, _I64, _PU64]),
+    "qmbx_hitlog_count": (ctypes.c_int, [_P, _P, _P]),
+    "qmbx_apply_within_logged": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _P, _P, _U64, _I64, _P]),
+    "qmbx_apply_within_f32c_logged": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _I32, _I32, _P, _P, _P, _U64,
+                                                     _I64, _P]),
+    "qmbx_apply_within_adjoint_logged": (ctypes.c_int, [_P, _P, _P, _U64, _I64, _I64, _I64, _I32, _P, _P, _P]),
+    "qmbx_apply_within_adjoint_f32c_logged": (ctypes.c_int, [_P, _P, _P, _U64, _I64, _I64, _I64, _I32, _I32, _P, _P,
+                                                             _P, _P]),
     "qmbx_matrix_workspace": (ctypes.c_int, [_P, _I64, _PU64]),
     "qmbx_matrix_count": (ctypes.c_int, [_P, _P, _P, _I64, _P, _PI64, _P, _U64, _P]),
     "qmbx_matrix_fill": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P, _U64, _P]),
@@ -66,9 +66,10 @@ SIGNATURES: dict[str, tuple] = {
     "qmbx_single_relative": (ctypes.c_int, [_P, _P, _P, _I64, _U64, _P, _P, _U64, _P]),
     "qmbx_sampler_log_amplitude": (ctypes.c_int, [_I64, _I32, _I32, _I32, _P, _P, _P, _P]),
     "qmbx_sampler_log_amplitude_grad": (ctypes.c_int, [_I64, _I32, _I32, _I32, _P, _P, _P, _P, _P]),
-    "qmbx_sampler_site": (ctypes.c_int, [_I64, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
-    "qmbx_sampler_take": (ctypes.c_int, [_I64, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+    "qmbx_sampler_site": (ctypes.c_int, [_I64, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                          _P]),
+    "qmbx_sampler_take": (ctypes.c_int, [_I64, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                         _P, _I64, _P]),
     "qmbx_profile_enable": (ctypes.c_int, [_I32]),
     "qmbx_profile_read": (ctypes.c_int, [_PI64, _PI64, ctypes.POINTER(ctypes.c_double)]),
 }

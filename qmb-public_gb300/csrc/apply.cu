@@ -636,19 +636,19 @@ struct ApplyArgs {
     int include_diag;
     HitLog log;       // forward calls: record the hits here (hits == NULL: no record)
     LogHead* log_head;   // and the walk's direction and row counts
-    int32_t* log_first;  // and, per configs_i row, its first row
     int64_t log_rows;    // diagonal records the replay reads: max(n_i, n_j)
 };
 
 // Launch one enumeration over the unique rows of `walk`: the grouped kernel
 // (warp per row) or the tiled kernel (thread per row), as choose_walk says.
 template <int W, class V>
-int launch_walk(const V& v, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
+int launch_walk(const V& v, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s,
+                int group = kGroupEnumerate) {
     UniqueRows<W> src{walk.keys, walk.unique};
     if (choose_walk(part, walk.n, false) == Walk::kGrouped) {
-        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+        QMBX_KERNEL(group, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
     } else {
-        QMBX_KERNEL(kGroupEnumerate, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+        QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
     }
     QMBX_LAUNCH_CHECK("apply_within enumeration");
     return QMBX_OK;
@@ -657,15 +657,16 @@ int launch_walk(const V& v, const HashRows& walk, const PartView& part, const Pa
 // Pass over the diagonal terms of every walked row (adds into res): grouped
 // or tiled, as choose_walk says.
 template <int W, class D>
-int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s) {
+int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const PartView& diag, cudaStream_t s,
+                int group = kGroupDiagonal) {
     if (diag.n == 0) return QMBX_OK;
     UniqueRows<W> src{walk.keys, walk.unique};
     PartView none = part;
     none.n = 0;
     if (choose_walk(diag, walk.n, false) == Walk::kGrouped) {
-        QMBX_KERNEL(kGroupDiagonal, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+        QMBX_KERNEL(group, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
     } else {
-        QMBX_KERNEL(kGroupDiagonal, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+        QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
     }
     QMBX_LAUNCH_CHECK("apply_within diagonal pass");
     return QMBX_OK;
@@ -675,11 +676,145 @@ int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const P
 // visitor's flush or hits) followed by a tiled pass over the diagonal terms.
 template <int W, class V, class D>
 int launch_pivot(const V& v, const D& dv, const HashRows& walk, const PartView& part, const PartView& diag,
-                 cudaStream_t s) {
+                 cudaStream_t s, int group = kGroupEnumerate, int diag_group = kGroupDiagonal) {
     UniqueRows<W> src{walk.keys, walk.unique};
-    QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, walk.count, walk.n, part));
+    QMBX_KERNEL(group, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, walk.count, walk.n, part));
     QMBX_LAUNCH_CHECK("apply_within pivot walk");
-    return launch_diag<W>(dv, walk, part, diag, s);
+    return launch_diag<W>(dv, walk, part, diag, s, diag_group);
+}
+
+// Whether apply_within walks its input side (scatter) or its output side:
+// the side with fewer rows, unless the sets are the same or QMBX_DETERMINISTIC
+// asks for fixed-order sums.
+bool apply_scatter(const ApplyArgs& a, int64_t n_in, int64_t n_out) {
+    return !deterministic_mode() && !a.same && 2 * n_in < n_out;
+}
+
+// The term part a walk in direction `scatter` reads.
+PartView walk_part_of(const ApplyArgs& a, bool scatter) {
+    return part_view(a.table_host, a.table_dev,
+                     scatter ? (a.adjoint ? QMBX_PART_ADJ : QMBX_PART_FWD) : (a.adjoint ? QMBX_PART_FWD : QMBX_PART_ADJ));
+}
+
+// The walks of apply_within over built row sets: amplitudes `val` per first
+// row of the input side, results into res per first row of the output side
+// (gather walks assign their rows' sums; scatter and pivot walks add, so the
+// caller clears res for them).  rows_gate (device int, or NULL): the walked
+// rows are the first *rows_gate of the walked set, so a launch can be made
+// conditional on device state without a host round trip.
+template <int W>
+int walk_apply(const ApplyArgs& a, const HashRows& in_set, const HashRows& out_set, const void* val, double2* res,
+               const int* rows_gate, cudaStream_t s, int group = kGroupEnumerate, int diag_group = kGroupDiagonal) {
+    const int64_t n_in = a.adjoint ? a.n_j : a.n_i;
+    const int64_t n_out = a.adjoint ? a.n_i : a.n_j;
+    int st = QMBX_OK;
+    PartView fwd = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
+    PartView adj = part_view(a.table_host, a.table_dev, QMBX_PART_ADJ);
+    PartView diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
+    const bool include_diag = a.prec == Prec::F64 || a.include_diag;
+    if (!include_diag) diag.n = 0;
+    const bool exact_order = deterministic_mode();
+    const bool scatter = apply_scatter(a, n_in, n_out);
+    // walk the input side (scatter) with forward terms for the forward map
+    // or daggered terms (conjugated) for the adjoint; walk the output side
+    // (gather) with daggered terms for the forward map or forward terms
+    // (conjugated) for the adjoint
+    const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
+    HashRows walk = scatter ? in_set : out_set;
+    const Walk kind = choose_walk(part, walk.n, !exact_order);
+    const bool pivot = kind == Walk::kPivot;
+    // a gated walk takes its row count from *rows_gate (0: nothing to walk)
+    if (rows_gate != nullptr) walk.count = const_cast<int*>(rows_gate);
+    const HashView look = scatter ? out_set.hash() : in_set.hash();
+    // the grouped kernel walks the changing terms and a tiled pass adds the
+    // diagonal ones
+    const bool grouped = kind == Walk::kGrouped;
+    PartView walk_diag = diag;
+    if (grouped) walk_diag.n = 0;
+    if (pivot) {
+#define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
+    {                                                                                                            \
+        PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res}; v.log = a.log;             \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;                           \
+        st = launch_pivot<W>(v, dv, walk, part, diag, s, group, diag_group);                                                        \
+    }
+        const bool f32 = a.prec == Prec::F32C;
+        if (scatter) {
+            if (a.adjoint) {
+                if (f32) QMBX_PIVOT_CASE(true, true, true) else QMBX_PIVOT_CASE(true, false, true)
+            } else {
+                if (f32) QMBX_PIVOT_CASE(false, true, true) else QMBX_PIVOT_CASE(false, false, true)
+            }
+        } else {
+            if (a.adjoint) {
+                if (f32) QMBX_PIVOT_CASE(true, true, false) else QMBX_PIVOT_CASE(true, false, false)
+            } else {
+                if (f32) QMBX_PIVOT_CASE(false, true, false) else QMBX_PIVOT_CASE(false, false, false)
+            }
+        }
+#undef QMBX_PIVOT_CASE
+    } else if (scatter) {
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            } else {
+                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            }
+        } else {
+            if (a.adjoint) {
+                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            } else {
+                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            }
+        }
+    } else {
+        if (a.prec == Prec::F64) {
+            if (a.adjoint) {
+                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            } else {
+                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            }
+        } else {
+            if (a.adjoint) {
+                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            } else {
+                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
+                st = launch_walk<W>(v, walk, part, walk_diag, s, group);
+            }
+        }
+    }
+    if (st != QMBX_OK) return st;
+    if (grouped && diag.n > 0) {
+        const bool f32 = a.prec == Prec::F32C;
+#define QMBX_DIAG_CASE(CONJ, F32, SCATTER)                                              \
+    {                                                                                   \
+        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;  \
+        st = launch_diag<W>(dv, walk, part, diag, s, diag_group);                                   \
+    }
+        if (scatter) {
+            if (a.adjoint) {
+                if (f32) QMBX_DIAG_CASE(true, true, true) else QMBX_DIAG_CASE(true, false, true)
+            } else {
+                if (f32) QMBX_DIAG_CASE(false, true, true) else QMBX_DIAG_CASE(false, false, true)
+            }
+        } else {
+            if (a.adjoint) {
+                if (f32) QMBX_DIAG_CASE(true, true, false) else QMBX_DIAG_CASE(true, false, false)
+            } else {
+                if (f32) QMBX_DIAG_CASE(false, true, false) else QMBX_DIAG_CASE(false, false, false)
+            }
+        }
+#undef QMBX_DIAG_CASE
+        if (st != QMBX_OK) return st;
+    }
+    return QMBX_OK;
 }
 
 // Forward maps amplitudes on configs_i (input side) to configs_j (output
@@ -736,120 +871,19 @@ int apply_impl(const ApplyArgs& a, Arena& ws, cudaStream_t s) {
         val = summed;
     }
 
-    PartView fwd = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
-    PartView adj = part_view(a.table_host, a.table_dev, QMBX_PART_ADJ);
-    PartView diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
-    const bool include_diag = a.prec == Prec::F64 || a.include_diag;
-    if (!include_diag) diag.n = 0;
-    const bool exact_order = deterministic_mode();
-    const bool scatter = !exact_order && !a.same && 2 * n_in < n_out;
-    // walk the input side (scatter) with forward terms for the forward map
-    // or daggered terms (conjugated) for the adjoint; walk the output side
-    // (gather) with daggered terms for the forward map or forward terms
-    // (conjugated) for the adjoint
-    const PartView& part = scatter ? (a.adjoint ? adj : fwd) : (a.adjoint ? fwd : adj);
-    const HashRows& walk = scatter ? in_set : out_set;
-    const Walk kind = choose_walk(part, walk.n, !exact_order);
-    const bool pivot = kind == Walk::kPivot;
-    if (scatter || pivot) QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
-    const HashView look = scatter ? out_set.hash() : in_set.hash();
+    const bool scatter = apply_scatter(a, n_in, n_out);
+    const HashRows& walked = scatter ? in_set : out_set;
+    if (scatter || choose_walk(walk_part_of(a, scatter), walked.n, !deterministic_mode()) == Walk::kPivot) {
+        QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_out * sizeof(double2), s));
+    }
     if (a.log.hits != nullptr) {
         // the record of this forward call: no diagonal records yet, the walk's
-        // direction and configs_i's first rows (the adjoint's output map)
-        // (every record the replay reads, not only the walked side's: the
-        // replay runs over max(n_i, n_j) of them)
+        // direction (every record the replay reads, not only the walked
+        // side's: the replay runs over max(n_i, n_j) of them)
         QMBX_CUDA_TRY(cudaMemsetAsync(a.log.diag_rows, 0xff, (size_t)a.log_rows * sizeof(int2), s));
         QMBX_KERNEL(kGroupOther, s, log_head_kernel<<<1, 1, 0, s>>>(a.log_head, scatter ? 0 : 1, a.n_i, a.n_j, a.log.cap));
-        QMBX_CUDA_TRY(cudaMemcpyAsync(a.log_first, rs_i.first, (size_t)a.n_i * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     }
-    // the grouped kernel walks the changing terms and a tiled pass adds the
-    // diagonal ones
-    const bool grouped = kind == Walk::kGrouped;
-    PartView walk_diag = diag;
-    if (grouped) walk_diag.n = 0;
-    if (pivot) {
-#define QMBX_PIVOT_CASE(CONJ, F32, SCATTER)                                                                      \
-    {                                                                                                            \
-        PivotHits<W, CONJ, F32, SCATTER> v{{}, look, val, walk.unique, part.coef, part.coef32, res}; v.log = a.log;             \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;                           \
-        st = launch_pivot<W>(v, dv, walk, part, diag, s);                                                        \
-    }
-        const bool f32 = a.prec == Prec::F32C;
-        if (scatter) {
-            if (a.adjoint) {
-                if (f32) QMBX_PIVOT_CASE(true, true, true) else QMBX_PIVOT_CASE(true, false, true)
-            } else {
-                if (f32) QMBX_PIVOT_CASE(false, true, true) else QMBX_PIVOT_CASE(false, false, true)
-            }
-        } else {
-            if (a.adjoint) {
-                if (f32) QMBX_PIVOT_CASE(true, true, false) else QMBX_PIVOT_CASE(true, false, false)
-            } else {
-                if (f32) QMBX_PIVOT_CASE(false, true, false) else QMBX_PIVOT_CASE(false, false, false)
-            }
-        }
-#undef QMBX_PIVOT_CASE
-    } else if (scatter) {
-        if (a.prec == Prec::F64) {
-            if (a.adjoint) {
-                Scatter<W, true, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            } else {
-                Scatter<W, false, false> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, 1, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            }
-        } else {
-            if (a.adjoint) {
-                Scatter<W, true, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            } else {
-                Scatter<W, false, true> v{{}, look, val, walk.unique, part.coef, part.coef32, diag.coef, diag.coef32, include_diag, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            }
-        }
-    } else {
-        if (a.prec == Prec::F64) {
-            if (a.adjoint) {
-                GatherF64<W, true> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            } else {
-                GatherF64<W, false> v{{}, look, (const double2*)val, part.coef, diag.coef, walk.unique, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            }
-        } else {
-            if (a.adjoint) {
-                GatherF32C<W, true> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            } else {
-                GatherF32C<W, false> v{{}, look, (const float2*)val, part.coef32, diag.coef32, a.include_diag, walk.unique, res}; v.log = a.log;
-                st = launch_walk<W>(v, walk, part, walk_diag, s);
-            }
-        }
-    }
-    if (st != QMBX_OK) return st;
-    if (grouped && diag.n > 0) {
-        const bool f32 = a.prec == Prec::F32C;
-#define QMBX_DIAG_CASE(CONJ, F32, SCATTER)                                              \
-    {                                                                                   \
-        DiagAdd<W, CONJ, F32, SCATTER> dv{{}, look, val, walk.unique, diag.coef, diag.coef32, res}; dv.log = a.log;  \
-        st = launch_diag<W>(dv, walk, part, diag, s);                                   \
-    }
-        if (scatter) {
-            if (a.adjoint) {
-                if (f32) QMBX_DIAG_CASE(true, true, true) else QMBX_DIAG_CASE(true, false, true)
-            } else {
-                if (f32) QMBX_DIAG_CASE(false, true, true) else QMBX_DIAG_CASE(false, false, true)
-            }
-        } else {
-            if (a.adjoint) {
-                if (f32) QMBX_DIAG_CASE(true, true, false) else QMBX_DIAG_CASE(true, false, false)
-            } else {
-                if (f32) QMBX_DIAG_CASE(false, true, false) else QMBX_DIAG_CASE(false, false, false)
-            }
-        }
-#undef QMBX_DIAG_CASE
-        if (st != QMBX_OK) return st;
-    }
+    if ((st = walk_apply<W>(a, in_set, out_set, val, res, nullptr, s)) != QMBX_OK) return st;
     QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_out, kThreads), kThreads, 0, s>>>(res, out_set.first, n_out, a.adjoint ? 1 : 0, a.out64, a.out32));
     QMBX_LAUNCH_CHECK("apply_finalize_kernel");
     return QMBX_OK;
@@ -1032,18 +1066,30 @@ namespace qmbx {
 namespace {
 
 struct LogLayout {
-    uint64_t count, dir, first, diag_rows, diag_val, res, hits, total;
+    uint64_t gate, diag_rows, diag_val, res, hits, ws, ws_bytes, total;
 };
 
-LogLayout log_layout(int64_t n_i, int64_t n_j, int64_t cap) {
-    LogLayout L;
+// Device flags of one adjoint replay, written by log_gate_kernel.
+struct LogGate {
+    int valid;   // the header is a logged forward's with these row counts and capacity
+    int replay;  // valid and the record holds every hit: replay it
+    int rows;    // valid and the record is incomplete: rows the adjoint walk takes (else 0)
+    int pad;
+};
+
+// The log buffer: header, gate, diagonal records, the adjoint's per-row
+// sums, cap hit records, then the forward's own workspace (its row sets,
+// which the adjoint reuses).
+int log_layout(const void* table_host, int64_t n_i, int64_t n_j, bool same, int64_t cap, LogLayout& L) {
+    uint64_t ws_bytes = 0;
+    int st = apply_within_workspace_for(table_host, n_i, same ? n_i : n_j, same, &ws_bytes);
+    if (st != QMBX_OK) return st;
+    if (same) n_j = n_i;
     Arena a(nullptr, 0);
-    L.count = 0;  // LogHead at the start of the header
-    L.dir = offsetof(LogHead, dir);
-    a.take<unsigned char>(256);
+    a.take<LogHead>(1);
+    L.gate = a.used;
+    a.take<LogGate>(1);
     const uint64_t nw = (uint64_t)(n_i > n_j ? n_i : n_j);
-    L.first = a.used;
-    a.take<int32_t>((uint64_t)(n_i > 0 ? n_i : 1));
     L.diag_rows = a.used;
     a.take<int2>(nw > 0 ? nw : 1);
     L.diag_val = a.used;
@@ -1052,31 +1098,61 @@ LogLayout log_layout(int64_t n_i, int64_t n_j, int64_t cap) {
     a.take<double2>((uint64_t)(n_i > 0 ? n_i : 1));
     L.hits = a.used;
     a.take<int4>((uint64_t)(cap > 0 ? cap : 1));
+    L.ws = a.used;
+    L.ws_bytes = ws_bytes;
+    a.take<unsigned char>(ws_bytes > 0 ? ws_bytes : 1);
     L.total = a.used;
-    return L;
+    return QMBX_OK;
 }
 
-int attach_log(ApplyArgs& a, void* log, uint64_t log_bytes, int64_t cap) {
+// Point the forward's log fields into the caller's log buffer; the forward
+// then runs on the workspace inside the buffer (ws, ws_bytes).
+int attach_log(ApplyArgs& a, void* log, uint64_t log_bytes, int64_t cap, void** ws, uint64_t* ws_bytes) {
     if (log == nullptr || reinterpret_cast<uintptr_t>(log) % QMBX_ALIGN != 0) {
         return fail(QMBX_ERR_ARGUMENT, "log must be a %d-byte aligned device buffer", QMBX_ALIGN);
     }
     if (cap < 0) return fail(QMBX_ERR_ARGUMENT, "log capacity must not be negative");
     const int64_t n_j = a.same ? a.n_i : a.n_j;
-    const LogLayout L = log_layout(a.n_i, n_j, cap);
+    LogLayout L;
+    int st = log_layout(a.table_host, a.n_i, n_j, a.same, cap, L);
+    if (st != QMBX_OK) return st;
     if (log_bytes < L.total) {
         return fail(QMBX_ERR_WORKSPACE, "a log of %lld hits on %lld x %lld rows needs %llu bytes", (long long)cap,
                     (long long)a.n_i, (long long)n_j, (unsigned long long)L.total);
     }
     char* b = static_cast<char*>(log);
+    a.log_head = reinterpret_cast<LogHead*>(b);
+    a.log.count = &a.log_head->count;
     a.log.hits = reinterpret_cast<int4*>(b + L.hits);
-    a.log.count = reinterpret_cast<unsigned long long*>(b + L.count);
     a.log.cap = cap;
     a.log.diag_rows = reinterpret_cast<int2*>(b + L.diag_rows);
     a.log.diag_val = reinterpret_cast<double2*>(b + L.diag_val);
-    a.log_head = reinterpret_cast<LogHead*>(b);
-    a.log_first = reinterpret_cast<int32_t*>(b + L.first);
     a.log_rows = a.n_i > n_j ? a.n_i : n_j;
+    *ws = b + L.ws;
+    *ws_bytes = L.ws_bytes;
     return QMBX_OK;
+}
+
+// Decide, on the device, how the adjoint is formed from the log: replayed
+// when the header matches and the record is complete, walked (rows = the
+// walked set's distinct rows) when it is incomplete, neither when the buffer
+// holds no matching log (the output is then NaN).
+__global__ void log_gate_kernel(const LogHead* __restrict__ h, int64_t n_i, int64_t n_j, int64_t cap,
+                                const int* __restrict__ walk_rows, LogGate* __restrict__ g) {
+    const bool valid = h->magic == kLogMagic && h->dir >= 0 && h->dir <= 2 && h->n_i == n_i && h->n_j == n_j &&
+                       h->cap == cap;
+    const bool complete = valid && h->count <= (unsigned long long)cap;
+    g->valid = valid ? 1 : 0;
+    g->replay = complete && h->dir != 2 ? 1 : 0;
+    g->rows = valid && !complete ? *walk_rows : 0;
+}
+
+__global__ void log_poison_kernel(const LogGate* __restrict__ g, int64_t n, double2* out64, float2* out32) {
+    if (g->valid) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (out64) out64[i] = make_double2(nan(""), nan(""));
+    if (out32) out32[i] = make_float2(nanf(""), nanf(""));
 }
 
 // res[out] += conj(s * coef) * g[in] for every recorded hit: out and in are
@@ -1088,75 +1164,128 @@ int attach_log(ApplyArgs& a, void* log, uint64_t log_bytes, int64_t cap) {
 // first sums its runs of equal output rows (a segmented shuffle scan) and
 // the last lane of a run adds the run's sum, one atomic pair per run instead
 // of one per record.  Lanes past n take part in the scan with nothing to add.
+//
+// The FP32 path keeps every product and the run sums in compensated FP32
+// (exact two-products, TwoSum combination of (leading, tail) pairs) and
+// converts to FP64 once per run: GB300 issues FP64 arithmetic at a small
+// fraction of the FP32 rate, and per-record FP64 adds and shuffles made the
+// FP64 pipe this kernel's bound.
+__device__ __forceinline__ void run_add_f32(CompSum& a, float s2, float c2) {
+    float e;
+    two_sum(a.s, s2, a.s, e);
+    a.c = __fadd_rn(a.c, __fadd_rn(c2, e));
+}
+
 template <bool F32>
-__global__ void log_adjoint_kernel(const int4* __restrict__ hits, int64_t n, const int* __restrict__ dir_p,
-                                   PartView fwd, PartView adj, const void* __restrict__ g,
-                                   double2* __restrict__ res) {
+__global__ void log_adjoint_kernel(const int4* __restrict__ hits, const LogHead* __restrict__ head,
+                                   const LogGate* __restrict__ gate, PartView fwd, PartView adj,
+                                   const void* __restrict__ g, double2* __restrict__ res) {
+    if (!gate->replay) return;
+    const int64_t n = (int64_t)head->count;  // <= the capacity the grid covers (gate->replay)
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= n) return;  // whole warps past n
     const int lane = threadIdx.x & 31;
     const bool live = i < n;
-    const int dir = *dir_p;
-    const int4 h = live ? hits[i] : make_int4(-1, -1, 0, 0);
+    const int dir = head->dir;
+    const int4 h = live ? __ldg(hits + i) : make_int4(-1, -1, 0, 0);
     const int64_t slot = h.z & 0x7fffffff;
     const int out = dir == 0 ? h.x : h.y;
     const int in = dir == 0 ? h.y : h.x;
-    double re = 0.0, im = 0.0;
-    if (!live) {
-    } else if (F32) {
-        const float4 cf = __ldg((dir == 0 ? fwd.coef32 : adj.coef32) + slot);
-        const float2 p = __ldg(static_cast<const float2*>(g) + in);
-        // conj(c) p with c = (cf.x + cf.y) + i (cf.z + cf.w): exact FP32 two-products, summed in FP64
-        float x1, e1, x2, e2;
-        two_prod(cf.x, p.x, x1, e1);
-        two_prod(cf.z, p.y, x2, e2);
-        float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fmul_rn(cf.y, p.x), __fmul_rn(cf.w, p.y)));
-        re = ((double)x1 + (double)x2) + (double)lo;
-        two_prod(cf.x, p.y, x1, e1);
-        two_prod(cf.z, p.x, x2, e2);
-        lo = __fadd_rn(__fsub_rn(e1, e2), __fsub_rn(__fmul_rn(cf.y, p.y), __fmul_rn(cf.w, p.x)));
-        im = ((double)x1 - (double)x2) + (double)lo;
-    } else {
-        const double2 cf = __ldg((dir == 0 ? fwd.coef : adj.coef) + slot);
-        const double2 p = __ldg(static_cast<const double2*>(g) + in);
-        re = cf.x * p.x + cf.y * p.y;
-        im = cf.x * p.y - cf.y * p.x;
-    }
-    if (h.z < 0) {
-        re = -re;
-        im = -im;
-    }
     // runs of equal `out` in lane order: run index = number of run heads up to this lane
     const unsigned full = 0xffffffffu;
     const int prev = __shfl_up_sync(full, out, 1);
     const unsigned heads = __ballot_sync(full, lane == 0 || prev != out);
     const int run = __popc(heads & (full >> (31 - lane)));
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const double r = __shfl_up_sync(full, re, off);
-        const double m = __shfl_up_sync(full, im, off);
-        const int k = __shfl_up_sync(full, run, off);
-        if (lane >= off && k == run) {
-            re += r;
-            im += m;
-        }
-    }
     const int next = __shfl_down_sync(full, run, 1);
-    if (live && (lane == 31 || next != run)) {
-        atomicAdd(&res[out].x, re);
-        atomicAdd(&res[out].y, im);
+    const bool last = live && (lane == 31 || next != run);
+    if (F32) {
+        CompSum re, im;
+        re.zero();
+        im.zero();
+        if (live) {
+            const float4 cf = __ldg((dir == 0 ? fwd.coef32 : adj.coef32) + slot);
+            const float2 p = __ldg(static_cast<const float2*>(g) + in);
+            // conj(c) p with c = (cf.x + cf.y) + i (cf.z + cf.w), sign (-1)^parity
+            const float sg = h.z < 0 ? -1.f : 1.f;
+            float x1, e1, x2, e2;
+            two_prod(sg * cf.x, p.x, x1, e1);
+            two_prod(sg * cf.z, p.y, x2, e2);
+            float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fmul_rn(sg * cf.y, p.x), __fmul_rn(sg * cf.w, p.y)));
+            re.add2(x1, lo);
+            re.add(x2);
+            two_prod(sg * cf.x, p.y, x1, e1);
+            two_prod(sg * cf.z, p.x, x2, e2);
+            lo = __fadd_rn(__fsub_rn(e1, e2), __fsub_rn(__fmul_rn(sg * cf.y, p.y), __fmul_rn(sg * cf.w, p.x)));
+            im.add2(x1, lo);
+            im.add(-x2);
+        }
+        if (dir != 0) {
+            // the walked rows were the inputs: neighbouring records add into different rows
+            if (live) {
+                atomicAdd(&res[out].x, re.value());
+                atomicAdd(&res[out].y, im.value());
+            }
+            return;
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float rs = __shfl_up_sync(full, re.s, off), rc = __shfl_up_sync(full, re.c, off);
+            const float is = __shfl_up_sync(full, im.s, off), ic = __shfl_up_sync(full, im.c, off);
+            const int k = __shfl_up_sync(full, run, off);
+            if (lane >= off && k == run) {
+                run_add_f32(re, rs, rc);
+                run_add_f32(im, is, ic);
+            }
+        }
+        if (last) {
+            atomicAdd(&res[out].x, re.value());
+            atomicAdd(&res[out].y, im.value());
+        }
+    } else {
+        double re = 0.0, im = 0.0;
+        if (live) {
+            const double2 cf = __ldg((dir == 0 ? fwd.coef : adj.coef) + slot);
+            const double2 p = __ldg(static_cast<const double2*>(g) + in);
+            re = cf.x * p.x + cf.y * p.y;
+            im = cf.x * p.y - cf.y * p.x;
+            if (h.z < 0) {
+                re = -re;
+                im = -im;
+            }
+        }
+        if (dir != 0) {
+            if (live) {
+                atomicAdd(&res[out].x, re);
+                atomicAdd(&res[out].y, im);
+            }
+            return;
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const double r = __shfl_up_sync(full, re, off);
+            const double m = __shfl_up_sync(full, im, off);
+            const int k = __shfl_up_sync(full, run, off);
+            if (lane >= off && k == run) {
+                re += r;
+                im += m;
+            }
+        }
+        if (last) {
+            atomicAdd(&res[out].x, re);
+            atomicAdd(&res[out].y, im);
+        }
     }
 }
 
 template <bool F32>
 __global__ void log_diag_adjoint_kernel(const int2* __restrict__ rows, const double2* __restrict__ vals, int64_t n,
-                                        const int* __restrict__ dir_p, const void* __restrict__ g,
-                                        double2* __restrict__ res) {
+                                        const LogHead* __restrict__ head, const LogGate* __restrict__ gate,
+                                        const void* __restrict__ g, double2* __restrict__ res) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !gate->replay) return;
     const int2 d = rows[i];
     if (d.y < 0) return;
-    const int dir = *dir_p;
+    const int dir = head->dir;
     const int out = dir == 0 ? d.x : d.y;
     const int in = dir == 0 ? d.y : d.x;
     const double2 v = vals[i];
@@ -1174,117 +1303,158 @@ __global__ void log_diag_adjoint_kernel(const int2* __restrict__ rows, const dou
     atomicAdd(&res[out].y, v.x * py - v.y * px);
 }
 
-int adjoint_from_log(const void* table_host, const void* table_dev, const void* log, uint64_t log_bytes, int64_t cap,
-                     int64_t n_i, int64_t n_j, bool f32, const void* g, double2* out64, float2* out32,
-                     int64_t* hits_needed, cudaStream_t s) {
-    clear_error();
-    int st = check_table(table_host, table_dev);
-    if (st != QMBX_OK) return st;
-    if (n_i < 0 || n_j < 0 || n_i >= (int64_t(1) << 31) || n_j >= (int64_t(1) << 31)) {
-        return fail(QMBX_ERR_ARGUMENT, "row counts out of range");
-    }
-    if (log == nullptr || reinterpret_cast<uintptr_t>(log) % QMBX_ALIGN != 0) {
-        return fail(QMBX_ERR_ARGUMENT, "log must be a %d-byte aligned device buffer", QMBX_ALIGN);
-    }
-    const LogLayout L = log_layout(n_i, n_j, cap);
-    if (log_bytes < L.total) return fail(QMBX_ERR_ARGUMENT, "log buffer smaller than its layout");
-    if (n_i > 0 && out64 == nullptr && out32 == nullptr) return fail(QMBX_ERR_ARGUMENT, "no output given");
-    if (n_j > 0 && g == nullptr) return fail(QMBX_ERR_ARGUMENT, "g_j must not be NULL");
-    const char* b = static_cast<const char*>(log);
-    LogHead head{};
-    QMBX_CUDA_TRY(cudaMemcpyAsync(&head, b, sizeof(head), cudaMemcpyDeviceToHost, s));
-    QMBX_CUDA_TRY(cudaStreamSynchronize(s));
-    if (head.magic != kLogMagic || head.dir < 0 || head.dir > 2) {
-        return fail(QMBX_ERR_ARGUMENT, "the buffer holds no hit log (no logged forward call wrote it)");
-    }
-    if (head.n_i != n_i || head.n_j != n_j || head.cap != cap) {
-        return fail(QMBX_ERR_ARGUMENT, "the log was written for %lld x %lld rows and %lld hits, not %lld x %lld and %lld",
-                    (long long)head.n_i, (long long)head.n_j, (long long)head.cap, (long long)n_i, (long long)n_j,
-                    (long long)cap);
-    }
-    if (hits_needed) *hits_needed = (int64_t)head.count;
-    if ((int64_t)head.count > cap) {
-        return fail(QMBX_ERR_WORKSPACE, "the log holds %lld of the forward's %llu hits", (long long)cap, head.count);
-    }
-    if (n_i == 0) return QMBX_OK;
-    if (head.dir == 2 || n_j == 0) {
-        if (out64) QMBX_CUDA_TRY(cudaMemsetAsync(out64, 0, (size_t)n_i * sizeof(double2), s));
-        if (out32) QMBX_CUDA_TRY(cudaMemsetAsync(out32, 0, (size_t)n_i * sizeof(float2), s));
-        return QMBX_OK;
-    }
-    double2* res = reinterpret_cast<double2*>(const_cast<char*>(b) + L.res);
-    const int* dir = reinterpret_cast<const int*>(b + L.dir);
+// The adjoint product g_j -> configs_i from a logged forward's buffer, with
+// no host round trip: a gate kernel reads the log's header on the device;
+// a complete record is replayed, an incomplete one (more hits than its
+// capacity) is replaced by the adjoint walk over the row sets the forward
+// left in the buffer; a buffer that holds no matching log gives NaN.
+template <int W>
+int adjoint_from_log_impl(const void* table_host, const void* table_dev, char* b, const LogLayout& L, int64_t cap,
+                          int64_t n_i, int64_t n_j, bool same, bool f32, int include_diag, const void* g,
+                          double2* out64, float2* out32, cudaStream_t s) {
+    Arena ws(b + L.ws, L.ws_bytes);
+    HashRows rs_i = take_hashrows<W>(ws, n_i);
+    HashRows rs_j = same ? rs_i : take_hashrows<W>(ws, n_j);
+    if (!ws.fits()) return fail(QMBX_ERR_ARGUMENT, "log buffer smaller than its layout");
+    const LogHead* head = reinterpret_cast<const LogHead*>(b);
+    LogGate* gate = reinterpret_cast<LogGate*>(b + L.gate);
+    double2* res = reinterpret_cast<double2*>(b + L.res);
+    // the adjoint walk the record stands in for: its walked set's distinct rows gate it
+    ApplyArgs a{table_host, table_dev, nullptr, n_i, nullptr, n_j, same, true, f32 ? Prec::F32C : Prec::F64,
+                g, out64, out32, include_diag, {}, nullptr, 0};
+    const bool scatter = apply_scatter(a, n_j, n_i);
+    const HashRows& walked = scatter ? rs_j : rs_i;
     QMBX_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)n_i * sizeof(double2), s));
+    QMBX_KERNEL(kGroupOther, s, log_gate_kernel<<<1, 1, 0, s>>>(head, n_i, n_j, cap, walked.count, gate));
     const PartView fwd = part_view(table_host, table_dev, QMBX_PART_FWD);
     const PartView adj = part_view(table_host, table_dev, QMBX_PART_ADJ);
-    const int64_t nh = (int64_t)head.count;
     const int64_t nw = n_i > n_j ? n_i : n_j;
     const int4* hits = reinterpret_cast<const int4*>(b + L.hits);
     const int2* drows = reinterpret_cast<const int2*>(b + L.diag_rows);
     const double2* dvals = reinterpret_cast<const double2*>(b + L.diag_val);
+    const int64_t ncap = cap > 0 ? cap : 1;
     if (f32) {
-        if (nh > 0) QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<true><<<grid_for(nh, kThreads), kThreads, 0, s>>>(hits, nh, dir, fwd, adj, g, res));
-        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<true><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, dir, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<true><<<grid_for(ncap, kThreads), kThreads, 0, s>>>(hits, head, gate, fwd, adj, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<true><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, head, gate, g, res));
     } else {
-        if (nh > 0) QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<false><<<grid_for(nh, kThreads), kThreads, 0, s>>>(hits, nh, dir, fwd, adj, g, res));
-        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<false><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, dir, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_adjoint_kernel<false><<<grid_for(ncap, kThreads), kThreads, 0, s>>>(hits, head, gate, fwd, adj, g, res));
+        QMBX_KERNEL(kGroupSpmv, s, log_diag_adjoint_kernel<false><<<grid_for(nw, kThreads), kThreads, 0, s>>>(drows, dvals, nw, head, gate, g, res));
     }
-    QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_i, kThreads), kThreads, 0, s>>>(res, reinterpret_cast<const int32_t*>(b + L.first), n_i, 1, out64, out32));
+    QMBX_LAUNCH_CHECK("adjoint from log");
+    // an incomplete record: the adjoint walk (its walked rows gated by the device count; 0 otherwise)
+    int st = walk_apply<W>(a, rs_j, rs_i, g, res, &gate->rows, s, kGroupSpmv, kGroupSpmv);
+    if (st != QMBX_OK) return st;
+    QMBX_KERNEL(kGroupOther, s, apply_finalize_kernel<<<grid_for(n_i, kThreads), kThreads, 0, s>>>(res, rs_i.first, n_i, 1, out64, out32));
+    QMBX_KERNEL(kGroupOther, s, log_poison_kernel<<<grid_for(n_i, kThreads), kThreads, 0, s>>>(gate, n_i, out64, out32));
     QMBX_LAUNCH_CHECK("adjoint from log");
     return QMBX_OK;
+}
+
+int adjoint_from_log(const void* table_host, const void* table_dev, const void* log, uint64_t log_bytes, int64_t cap,
+                     int64_t n_i, int64_t n_j, bool same, bool f32, int include_diag, const void* g, double2* out64,
+                     float2* out32, cudaStream_t s) {
+    clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
+    if (same) n_j = n_i;
+    if (n_i < 0 || n_j < 0 || n_i >= (int64_t(1) << 31) || n_j >= (int64_t(1) << 31) || cap < 0) {
+        return fail(QMBX_ERR_ARGUMENT, "row counts or capacity out of range");
+    }
+    if (log == nullptr || reinterpret_cast<uintptr_t>(log) % QMBX_ALIGN != 0) {
+        return fail(QMBX_ERR_ARGUMENT, "log must be a %d-byte aligned device buffer", QMBX_ALIGN);
+    }
+    LogLayout L;
+    if ((st = log_layout(table_host, n_i, n_j, same, cap, L)) != QMBX_OK) return st;
+    if (log_bytes < L.total) return fail(QMBX_ERR_ARGUMENT, "log buffer smaller than its layout");
+    if (n_i > 0 && out64 == nullptr && out32 == nullptr) return fail(QMBX_ERR_ARGUMENT, "no output given");
+    if (n_j > 0 && g == nullptr) return fail(QMBX_ERR_ARGUMENT, "g_j must not be NULL");
+    if (n_i == 0) return QMBX_OK;
+    if (n_j == 0) {
+        if (out64) QMBX_CUDA_TRY(cudaMemsetAsync(out64, 0, (size_t)n_i * sizeof(double2), s));
+        if (out32) QMBX_CUDA_TRY(cudaMemsetAsync(out32, 0, (size_t)n_i * sizeof(float2), s));
+        return QMBX_OK;
+    }
+    char* b = static_cast<char*>(const_cast<void*>(log));
+    switch (header_of(table_host)->n_words) {
+        case 1: return adjoint_from_log_impl<1>(table_host, table_dev, b, L, cap, n_i, n_j, same, f32, include_diag, g, out64, out32, s);
+        case 2: return adjoint_from_log_impl<2>(table_host, table_dev, b, L, cap, n_i, n_j, same, f32, include_diag, g, out64, out32, s);
+        case 3: return adjoint_from_log_impl<3>(table_host, table_dev, b, L, cap, n_i, n_j, same, f32, include_diag, g, out64, out32, s);
+        case 4: return adjoint_from_log_impl<4>(table_host, table_dev, b, L, cap, n_i, n_j, same, f32, include_diag, g, out64, out32, s);
+        default: return fail(QMBX_ERR_ARGUMENT, "unsupported word count");
+    }
 }
 
 }  // namespace
 }  // namespace qmbx
 
-extern "C" int qmbx_hitlog_bytes(int64_t n_i, int64_t n_j, int64_t cap, uint64_t* bytes) {
+extern "C" int qmbx_hitlog_bytes(const void* table_host, int64_t n_i, int64_t n_j, int32_t same_configs, int64_t cap,
+                                 uint64_t* bytes) {
     clear_error();
     if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
     if (n_i < 0 || n_j < 0 || cap < 0) return fail(QMBX_ERR_ARGUMENT, "sizes must not be negative");
-    *bytes = log_layout(n_i, n_j, cap).total;
+    const qmbx_table_header* h = header_of(table_host);
+    if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
+    LogLayout L;
+    int st = log_layout(table_host, n_i, n_j, same_configs != 0, cap, L);
+    if (st != QMBX_OK) return st;
+    *bytes = L.total;
+    return QMBX_OK;
+}
+
+extern "C" int qmbx_hitlog_count(const void* log, unsigned long long* count, qmbx_stream_t stream) {
+    clear_error();
+    if (log == nullptr || count == nullptr) return fail(QMBX_ERR_ARGUMENT, "pointers must not be NULL");
+    QMBX_CUDA_TRY(cudaMemcpyAsync(count, &static_cast<const LogHead*>(log)->count, sizeof(unsigned long long),
+                                  cudaMemcpyDefault, reinterpret_cast<cudaStream_t>(stream)));
     return QMBX_OK;
 }
 
 extern "C" int qmbx_apply_within_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
                                         const double* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
-                                        int32_t same_configs, double* psi_j, void* workspace, uint64_t workspace_bytes,
-                                        void* log, uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream) {
+                                        int32_t same_configs, double* psi_j, void* log, uint64_t log_bytes,
+                                        int64_t log_cap, qmbx_stream_t stream) {
     clear_error();
-    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F64,
-                psi_i, reinterpret_cast<double2*>(psi_j), nullptr, 1, {}, nullptr, nullptr, 0};
-    int st = attach_log(a, log, log_bytes, log_cap);
+    int st = check_table(table_host, table_dev);
     if (st != QMBX_OK) return st;
-    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+    ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F64,
+                psi_i, reinterpret_cast<double2*>(psi_j), nullptr, 1, {}, nullptr, 0};
+    void* ws = nullptr;
+    uint64_t ws_bytes = 0;
+    if ((st = attach_log(a, log, log_bytes, log_cap, &ws, &ws_bytes)) != QMBX_OK) return st;
+    return run_apply(a, ws, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int qmbx_apply_within_f32c_logged(const void* table_host, const void* table_dev, const uint8_t* configs_i,
                                              const float* psi_i, int64_t n_i, const uint8_t* configs_j, int64_t n_j,
                                              int32_t same_configs, int32_t include_diagonal, double* out_f64,
-                                             float* out_f32, void* workspace, uint64_t workspace_bytes, void* log,
-                                             uint64_t log_bytes, int64_t log_cap, qmbx_stream_t stream) {
+                                             float* out_f32, void* log, uint64_t log_bytes, int64_t log_cap,
+                                             qmbx_stream_t stream) {
     clear_error();
+    int st = check_table(table_host, table_dev);
+    if (st != QMBX_OK) return st;
     ApplyArgs a{table_host, table_dev, configs_i, n_i, configs_j, n_j, same_configs != 0, false, Prec::F32C,
                 psi_i, reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), include_diagonal,
-                {}, nullptr, nullptr, 0};
-    int st = attach_log(a, log, log_bytes, log_cap);
-    if (st != QMBX_OK) return st;
-    return run_apply(a, workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+                {}, nullptr, 0};
+    void* ws = nullptr;
+    uint64_t ws_bytes = 0;
+    if ((st = attach_log(a, log, log_bytes, log_cap, &ws, &ws_bytes)) != QMBX_OK) return st;
+    return run_apply(a, ws, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int qmbx_apply_within_adjoint_logged(const void* table_host, const void* table_dev, const void* log,
                                                 uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
-                                                const double* g_j, double* out_i, int64_t* hits_needed,
+                                                int32_t same_configs, const double* g_j, double* out_i,
                                                 qmbx_stream_t stream) {
-    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, false, g_j,
-                            reinterpret_cast<double2*>(out_i), nullptr, hits_needed,
-                            reinterpret_cast<cudaStream_t>(stream));
+    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, same_configs != 0, false, 1,
+                            g_j, reinterpret_cast<double2*>(out_i), nullptr, reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int qmbx_apply_within_adjoint_f32c_logged(const void* table_host, const void* table_dev, const void* log,
                                                      uint64_t log_bytes, int64_t log_cap, int64_t n_i, int64_t n_j,
+                                                     int32_t same_configs, int32_t include_diagonal,
                                                      const float* g_j, double* out_f64, float* out_f32,
-                                                     int64_t* hits_needed, qmbx_stream_t stream) {
-    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, true, g_j,
-                            reinterpret_cast<double2*>(out_f64), reinterpret_cast<float2*>(out_f32), hits_needed,
-                            reinterpret_cast<cudaStream_t>(stream));
+                                                     qmbx_stream_t stream) {
+    return adjoint_from_log(table_host, table_dev, log, log_bytes, log_cap, n_i, n_j, same_configs != 0, true,
+                            include_diagonal, g_j, reinterpret_cast<double2*>(out_f64),
+                            reinterpret_cast<float2*>(out_f32), reinterpret_cast<cudaStream_t>(stream));
 }

@@ -764,16 +764,22 @@ struct GroupCursor {
     }
 };
 
+// Walk the groups of part pv that row c reaches; with split > 1, only every
+// split-th of them, starting at the part-th (a row shared by split warps).
 template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
-                                          int lane, HitQueue& hq) {
+                                          int lane, HitQueue& hq, int part = 0, int split = 1) {
     if (pv.n == 0) return;
     GroupCursor<W> cur;
     cur.start(c);
     int64_t g;
+    int seq = 0;  // groups yielded so far (split walks)
     if (pv.wide) {
 #pragma unroll 1
-        while (cur.next(g, c, pv)) walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
+        while (cur.next(g, c, pv)) {
+            if (split > 1 && (seq++ % split) != part) continue;
+            walk_group_lanes<W, DIAG>(v, acc, c, pv, g, lane, hq);
+        }
     } else {
         // small groups: the cursor deals 32 groups to the lanes, one each,
         // then every lane walks its group (all 32 at once)
@@ -781,6 +787,7 @@ __device__ __forceinline__ void walk_part(const V& v, typename V::Acc& acc, cons
         int64_t mine = -1;
 #pragma unroll 1
         while (cur.next(g, c, pv)) {
+            if (split > 1 && (seq++ % split) != part) continue;
             if (k == lane) mine = g;
             if (++k == 32) {
                 walk_group_serial<W, DIAG>(v, acc, c, pv, mine);
@@ -818,6 +825,39 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
             queue_drain(v, acc, hq, lane, true);
         }
         walk_part<W, true>(v, acc, c, diag, lane, hq);
+        v.reduce(acc);
+        if (lane == 0) v.finish(acc, row, c);
+    }
+    __syncthreads();
+    v.block_flush(sh);
+}
+
+// The grouped walk with each row's groups shared by `split` warps (warp
+// item u walks row u / split, every split-th group from the (u % split)-th):
+// for visitors whose per-row work adds up across parts of a row (the
+// find_relative passes), when there are too few rows to fill the GPU with
+// one warp each.  Each part gets its own init / reduce / finish.
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads) grouped_split_kernel(V v, Src src, int64_t n, int split, PartView off,
+                                                                 PartView diag) {
+    __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
+    __shared__ int2 hitq[kWarpsPerBlock][64];
+    static_assert(!V::kBatched, "split walks serve visitors that handle each term in place");
+    v.block_init(sh);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t items = n * split;
+    const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t u = (int64_t)blockIdx.x * kWarpsPerBlock + warp; u < items; u += stride) {
+        const int64_t row = u / split;
+        const int part = (int)(u - row * split);
+        const Key<W> c = src.get(row);
+        typename V::Acc acc;
+        v.init(acc, row, c, sh);
+        HitQueue hq{hitq[warp], 0, nullptr, nullptr, 0};
+        walk_part<W, false>(v, acc, c, off, lane, hq, part, split);
+        walk_part<W, true>(v, acc, c, diag, lane, hq, part, split);
         v.reduce(acc);
         if (lane == 0) v.finish(acc, row, c);
     }
@@ -973,6 +1013,11 @@ __global__ void __launch_bounds__(kThreads) pivot_kernel(V v, Src src, const int
 // Grid for pivot_kernel: a few resident blocks per SM, looping over work items.
 int pivot_grid();
 
+// Warps a row's groups are shared by in grouped_split_kernel: enough for
+// about two waves of warps over n_rows rows, at most 16 (1 when the rows
+// fill the GPU alone).
+int row_split(int64_t n_rows);
+
 // Which kernel walks a term part over n_rows rows:
 //   pivot    parts of kGroupedMinTerms terms or more whose non-empty groups
 //            hold kPivotMeanGroup terms or more on average (when the caller
@@ -982,12 +1027,15 @@ int pivot_grid();
 //            groups are large), where a thread per row would leave most of
 //            the GPU idle;
 //   tiled    small parts over more rows (e.g. the diagonal parts, whose
-//            groups hold one term or two, over 20,000 rows).
+//            groups hold one term or two, over 20,000 rows), and parts of up
+//            to kTiledMaxTerms terms in groups of a few terms over
+//            kFewWideRows rows or more.
 // QMBX_WALK=pivot, grouped or tiled in the environment forces a kernel
 // (read at every call; pivot falls back to grouped where it cannot serve).
 constexpr int kPivotMeanGroup = 300;
 constexpr int64_t kFewRows = 8192;
 constexpr int64_t kFewWideRows = 65536;
+constexpr int64_t kTiledMaxTerms = 8192;
 enum class Walk { kTiled, kGrouped, kPivot };
 Walk choose_walk(const PartView& part, int64_t n_rows, bool pivot_ok);
 

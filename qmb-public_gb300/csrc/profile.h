@@ -8,7 +8,9 @@ namespace qmbx {
 // kGroupEnumerate is the main term walk; kGroupDiagonal the separate
 // passes over diagonal terms that follow it; kGroupSort the radix sorts
 // (histogram, scan and scatter passes); kGroupSpmv the products with a
-// materialised matrix and the adjoint products replayed from a hit log
+// materialised matrix and the adjoint products formed from a hit log (the
+// replay, and the adjoint walk that stands in for an incomplete record,
+// launched every time and walking no row when the record is complete)
 enum ProfileGroup {
     kGroupEnumerate = 0,
     kGroupKeys = 1,

@@ -228,7 +228,13 @@ int launch_relative(const RelativeArgs& r, const uint64_t* keys_i, int64_t n_i, 
     KeyRows<W> src{keys_i};
     const Walk kind = choose_walk(r.off, n_i, true);
     if (kind == Walk::kGrouped) {
-        QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
+        // few rows (the sampled threshold pass, small seed sets): a row's groups shared by several warps
+        const int split = row_split(n_i);
+        if (split > 1) {
+            QMBX_KERNEL(kGroupEnumerate, s, grouped_split_kernel<W><<<grouped_grid(n_i * split), kThreads, 0, s>>>(v, src, n_i, split, r.off, r.diag));
+        } else {
+            QMBX_KERNEL(kGroupEnumerate, s, grouped_kernel<W><<<grouped_grid(n_i), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off, r.diag));
+        }
     } else if (kind == Walk::kPivot) {
         // pivot-major walk of the changing terms, then the diagonal terms tiled
         QMBX_KERNEL(kGroupEnumerate, s, pivot_kernel<W><<<pivot_grid(), kThreads, 0, s>>>(v, src, nullptr, n_i, r.off));

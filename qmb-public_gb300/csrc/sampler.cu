@@ -12,6 +12,7 @@
 // same for down (qmb/mlp.py _mask).  Disallowed entries get log amplitude
 // -inf.  Arithmetic is FP32 as in the reference (the network's dtype).
 #include <cuda_runtime.h>
+#include <float.h>
 #include <math.h>
 
 #include "device.cuh"
@@ -28,15 +29,19 @@ __device__ __forceinline__ void site_mask(int i, int sites, int up, int down, in
     ok[3] = up1 && dn1;
 }
 
-// The masked log amplitudes d[k] shifted by log(sum_k exp(2 d[k])) / 2.
+// The masked log amplitudes d[k] shifted by log(sum_k exp(2 d[k])) / 2.  The
+// four terms are summed as (e0 + e1) + (e2 + e3), the order torch's CUDA sum
+// over a row of four takes, so that the values match the reference's torch
+// expression bit for bit on the GPU.
 __device__ __forceinline__ void normalized(const float4 raw, const bool (&ok)[4], float (&nd)[4]) {
     float d[4] = {raw.x, raw.y, raw.z, raw.w};
-    float sum = 0.f;
+    float e[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         d[k] = ok[k] ? d[k] : -INFINITY;
-        sum += expf(2.f * d[k]);
+        e[k] = expf(2.f * d[k]);
     }
+    const float sum = __fadd_rn(__fadd_rn(e[0], e[1]), __fadd_rn(e[2], e[3]));
     const float shift = logf(sum) / 2.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) nd[k] = d[k] - shift;
@@ -94,15 +99,21 @@ __global__ void log_amplitude_grad_kernel(int64_t rows, int sites, int up, int d
 //   l_k = lp + 2 nd_k,  G_k = l_k - log(-log u_k),  Z = max_k G_k,
 //   t_k = -log(exp(-gp) - exp(-Z) + exp(-G_k)),
 // written child-major (child k of row r at k * n + r), as the reference
-// lays out its four appended copies.  With la (the rows' log amplitudes so
+// lays out its four appended copies.  Rows whose gp is not finite have no
+// children (all four -inf).  With la (the rows' log amplitudes so
 // far, FP64) the children's a_k = la + nd_k are written too: after the last
 // site they are the log amplitudes the network's forward gives the sampled
 // configurations (the same FP32 terms summed in FP64 in the same order).
+// With `bad` (a device counter the caller zeroes), a child whose value is
+// NaN or +inf is written as -FLT_MAX and counted: the reference's descending
+// sort puts such values first and then drops them, so they take places of
+// the cut without being kept; sampler_take_kernel marks the places they took.
 __global__ void sampler_site_kernel(int64_t n, int site, int sites, int up, int down, const float4* __restrict__ delta,
                                     const int2* __restrict__ counts, const float* __restrict__ lp,
                                     const float* __restrict__ gp, const float4* __restrict__ uniforms,
                                     float* __restrict__ l_out, float* __restrict__ t_out,
-                                    const double* __restrict__ la, double* __restrict__ a_out) {
+                                    const double* __restrict__ la, double* __restrict__ a_out,
+                                    int* __restrict__ bad) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int2 c = counts[r];
@@ -122,11 +133,21 @@ __global__ void sampler_site_kernel(int64_t n, int site, int sites, int up, int 
         z = fmaxf(z, g[k]);
     }
     const float ep = expf(-parent), ez = expf(-z);
+    // a row carried with a value that is not finite is one the reference has
+    // dropped (its selection keeps finite values only): no children
+    const bool dead = !isfinite(parent);
+    int n_bad = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        l_out[k * n + r] = l[k];
-        t_out[k * n + r] = -logf(ep - ez + expf(-g[k]));
+        float t = dead ? -INFINITY : -logf(ep - ez + expf(-g[k]));
+        if (bad != nullptr && (isnan(t) || t == INFINITY)) {
+            t = -FLT_MAX;
+            ++n_bad;
+        }
+        l_out[k * n + r] = dead ? -INFINITY : l[k];
+        t_out[k * n + r] = t;
     }
+    if (n_bad) atomicAdd(bad, n_bad);
     if (la != nullptr) {
         const double a = la[r];
 #pragma unroll
@@ -137,13 +158,17 @@ __global__ void sampler_site_kernel(int64_t n, int site, int sites, int up, int 
 // The m chosen children (index = k * n + parent): their occupations (the
 // parent's, site `site` set to k), network inputs, electron counts and
 // log probabilities.  occ/xf are [rows][sites] and [rows][2 sites].
+// With `bad` (the site kernel's count of NaN / +inf values), the chosen rows
+// the reference would not keep get gp -inf: those written as -FLT_MAX, and
+// those past batch - *bad (the places the reference's NaN / +inf values
+// took at the top of its sort).
 __global__ void sampler_take_kernel(int64_t m, int64_t n, int site, int sites, const int64_t* __restrict__ index,
                                     const uint8_t* __restrict__ occ_in, const int2* __restrict__ counts_in,
                                     const float* __restrict__ l_in, const float* __restrict__ t_in,
                                     uint8_t* __restrict__ occ_out, float* __restrict__ xf_out,
                                     int2* __restrict__ counts_out, float* __restrict__ lp_out,
                                     float* __restrict__ gp_out, const double* __restrict__ a_in,
-                                    double* __restrict__ la_out) {
+                                    double* __restrict__ la_out, int64_t batch, const int* __restrict__ bad) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
     const int64_t idx = index[j];
@@ -161,7 +186,9 @@ __global__ void sampler_take_kernel(int64_t m, int64_t n, int site, int sites, c
     const int2 c = counts_in[parent];
     counts_out[j] = make_int2(c.x + (k >> 1), c.y + (k & 1));
     lp_out[j] = l_in[idx];
-    gp_out[j] = t_in[idx];
+    const float t = t_in[idx];
+    const bool dropped = bad != nullptr && (t == -FLT_MAX || j >= batch - (int64_t)*bad);
+    gp_out[j] = dropped ? -INFINITY : t;
     if (a_in != nullptr) la_out[j] = a_in[idx];
 }
 
@@ -212,7 +239,7 @@ extern "C" int qmbx_sampler_log_amplitude_grad(int64_t rows, int32_t sites, int3
 extern "C" int qmbx_sampler_site(int64_t n, int32_t site, int32_t sites, int32_t spin_up, int32_t spin_down,
                                  const float* delta, const int32_t* counts, const float* lp, const float* gp,
                                  const float* uniforms, float* l_out, float* t_out, const double* la,
-                                 double* a_out, qmbx_stream_t stream) {
+                                 double* a_out, int32_t* bad, qmbx_stream_t stream) {
     clear_error();
     int st = check_sites(sites, spin_up, spin_down);
     if (st != QMBX_OK) return st;
@@ -224,7 +251,7 @@ extern "C" int qmbx_sampler_site(int64_t n, int32_t site, int32_t sites, int32_t
     }
     if ((la == nullptr) != (a_out == nullptr)) return fail(QMBX_ERR_ARGUMENT, "la and a_out go together");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    QMBX_KERNEL(kGroupOther, s, sampler_site_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, site, sites, spin_up, spin_down, reinterpret_cast<const float4*>(delta), reinterpret_cast<const int2*>(counts), lp, gp, reinterpret_cast<const float4*>(uniforms), l_out, t_out, la, a_out));
+    QMBX_KERNEL(kGroupOther, s, sampler_site_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, site, sites, spin_up, spin_down, reinterpret_cast<const float4*>(delta), reinterpret_cast<const int2*>(counts), lp, gp, reinterpret_cast<const float4*>(uniforms), l_out, t_out, la, a_out, bad));
     QMBX_LAUNCH_CHECK("sampler_site_kernel");
     return QMBX_OK;
 }
@@ -233,7 +260,7 @@ extern "C" int qmbx_sampler_take(int64_t m, int64_t n, int32_t site, int32_t sit
                                  const uint8_t* occ_in, const int32_t* counts_in, const float* l_in,
                                  const float* t_in, uint8_t* occ_out, float* xf_out, int32_t* counts_out,
                                  float* lp_out, float* gp_out, const double* a_in, double* la_out,
-                                 qmbx_stream_t stream) {
+                                 int64_t batch, const int32_t* bad, qmbx_stream_t stream) {
     clear_error();
     if (sites < 1 || site < 0 || site >= sites) return fail(QMBX_ERR_ARGUMENT, "site %d of %d out of range", site, sites);
     if (m < 0 || n < 0 || m > 4 * n) return fail(QMBX_ERR_ARGUMENT, "row counts out of range");
@@ -243,7 +270,7 @@ extern "C" int qmbx_sampler_take(int64_t m, int64_t n, int32_t site, int32_t sit
     }
     if ((a_in == nullptr) != (la_out == nullptr)) return fail(QMBX_ERR_ARGUMENT, "a_in and la_out go together");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    QMBX_KERNEL(kGroupOther, s, sampler_take_kernel<<<grid_for(m, kThreads), kThreads, 0, s>>>(m, n, site, sites, index, occ_in, reinterpret_cast<const int2*>(counts_in), l_in, t_in, occ_out, xf_out, reinterpret_cast<int2*>(counts_out), lp_out, gp_out, a_in, la_out));
+    QMBX_KERNEL(kGroupOther, s, sampler_take_kernel<<<grid_for(m, kThreads), kThreads, 0, s>>>(m, n, site, sites, index, occ_in, reinterpret_cast<const int2*>(counts_in), l_in, t_in, occ_out, xf_out, reinterpret_cast<int2*>(counts_out), lp_out, gp_out, a_in, la_out, batch, bad));
     QMBX_LAUNCH_CHECK("sampler_take_kernel");
     return QMBX_OK;
 }

@@ -222,9 +222,20 @@ class Hamiltonian:
     hit_log = True
 
     def _log_capacity(self, n_i: int, n_j: int, device: torch.device) -> int:
-        cap = self._log_caps.get((device.index, n_i, n_j), self._LOG_FIRST_GUESS)
-        free, _ = torch.cuda.mem_get_info(device)
-        return int(min(cap, free // 8 // 16))
+        """Hit records to reserve for a logged forward on rows of this shape: a first guess, then 1.25x
+        the count of the last call of this shape whose count has arrived (read without waiting)."""
+        key = (device.index, n_i, n_j)
+        state = self._log_caps.get(key)
+        if state is None:
+            free, _ = torch.cuda.mem_get_info(device)
+            state = self._log_caps[key] = {"cap": int(min(self._LOG_FIRST_GUESS, free // 8 // 16)), "pending": None}
+        pending = state["pending"]
+        if pending is not None and pending[1].query():
+            count = int(pending[0][0])
+            state["pending"] = None
+            if count > state["cap"] or count < state["cap"] // 4:
+                state["cap"] = int(count * 1.25) + 1024
+        return state["cap"]
 
     def _apply(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor, *, adjoint: bool,
                out_dtype: torch.dtype | None = None, include_diagonal: bool = True, log: bool = False):
@@ -246,19 +257,23 @@ class Hamiltonian:
         table = self._table(device, nq)
         same = int(configs_i.data_ptr() == configs_j.data_ptr() and n_i == n_j)
         lib = _native.library()
-        need = ctypes.c_uint64(0)
-        _native.check(lib.qmbx_apply_within_workspace(table.h, n_i, n_j, ctypes.byref(need)))
         with torch.cuda.device(device):
-            ws = _workspace(need.value, device)
+            ws = None
+            if not (log and not adjoint):
+                need = ctypes.c_uint64(0)
+                _native.check(lib.qmbx_apply_within_workspace(table.h, n_i, n_j, ctypes.byref(need)))
+                ws = _workspace(need.value, device)
             stream = _stream(device)
             record = None
             log_args = ()
             if log and not adjoint:
+                # the log holds the hit records and the forward's own workspace (its row sets are the
+                # adjoint's), so the forward takes no separate workspace
                 cap = self._log_capacity(n_i, n_j, device)
                 nbytes = ctypes.c_uint64(0)
-                _native.check(lib.qmbx_hitlog_bytes(n_i, n_j, cap, ctypes.byref(nbytes)))
+                _native.check(lib.qmbx_hitlog_bytes(table.h, n_i, n_j, same, cap, ctypes.byref(nbytes)))
                 buf = _workspace(nbytes.value, device)
-                record = _HitRecord(table, buf, cap, n_i, n_j, psi.dtype, include_diagonal)
+                record = _HitRecord(table, buf, cap, n_i, n_j, same, psi.dtype, include_diagonal)
                 log_args = (buf.data_ptr(), buf.numel(), cap)
             if psi.dtype == torch.complex128:
                 out = torch.empty(n_out, dtype=torch.complex128, device=device)
@@ -266,10 +281,12 @@ class Hamiltonian:
                     _native.call("qmbx_apply_within_adjoint", table.h, table.d, configs_i.data_ptr(), n_i,
                                  configs_j.data_ptr(), psi.data_ptr(), n_j, same, out.data_ptr(), ws.data_ptr(),
                                  ws.numel(), stream)
+                elif record:
+                    _native.call("qmbx_apply_within_logged", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(),
+                                 n_i, configs_j.data_ptr(), n_j, same, out.data_ptr(), *log_args, stream)
                 else:
-                    _native.call("qmbx_apply_within_logged" if record else "qmbx_apply_within", table.h, table.d,
-                                 configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j, same,
-                                 out.data_ptr(), ws.data_ptr(), ws.numel(), *log_args, stream)
+                    _native.call("qmbx_apply_within", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i,
+                                 configs_j.data_ptr(), n_j, same, out.data_ptr(), ws.data_ptr(), ws.numel(), stream)
                 out = out if out_dtype in (None, torch.complex128) else out.to(out_dtype)
                 return (out, record) if log and not adjoint else out
             want64 = out_dtype == torch.complex128
@@ -279,45 +296,49 @@ class Hamiltonian:
                 _native.call("qmbx_apply_within_adjoint_f32c", table.h, table.d, configs_i.data_ptr(), n_i,
                              configs_j.data_ptr(), psi.data_ptr(), n_j, same, int(include_diagonal), o64, o32,
                              ws.data_ptr(), ws.numel(), stream)
+            elif record:
+                _native.call("qmbx_apply_within_f32c_logged", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(),
+                             n_i, configs_j.data_ptr(), n_j, same, int(include_diagonal), o64, o32, *log_args, stream)
             else:
-                _native.call("qmbx_apply_within_f32c_logged" if record else "qmbx_apply_within_f32c", table.h,
-                             table.d, configs_i.data_ptr(), psi.data_ptr(), n_i, configs_j.data_ptr(), n_j, same,
-                             int(include_diagonal), o64, o32, ws.data_ptr(), ws.numel(), *log_args, stream)
+                _native.call("qmbx_apply_within_f32c", table.h, table.d, configs_i.data_ptr(), psi.data_ptr(), n_i,
+                             configs_j.data_ptr(), n_j, same, int(include_diagonal), o64, o32, ws.data_ptr(),
+                             ws.numel(), stream)
             return (out, record) if log and not adjoint else out
 
     def _adjoint_from_log(self, record: "_HitRecord", g: torch.Tensor,
-                          out_dtype: torch.dtype | None = None) -> torch.Tensor | None:
-        """The adjoint product of a logged forward call for g on its output rows, or None when the
-        record is incomplete (the capacity for rows of this shape is raised for the next call)."""
+                          out_dtype: torch.dtype | None = None) -> torch.Tensor:
+        """The adjoint product of a logged forward call for g on its output rows.
+
+        Nothing waits for the device: the library replays the record, or walks the adjoint when the
+        forward found more hits than the record holds.  The hit count is copied back without
+        waiting and sizes the next log of this shape."""
         device = record.buf.device
         g = g.to(record.dtype).contiguous()
         if g.shape != (record.n_j,):
             raise RuntimeError(f"g must have shape [{record.n_j}].")
-        needed = ctypes.c_int64(0)
-        lib = _native.library()
         table = record.table
         with torch.cuda.device(device):
             stream = _stream(device)
             if record.dtype == torch.complex128:
                 out = torch.empty(record.n_i, dtype=torch.complex128, device=device)
-                status = lib.qmbx_apply_within_adjoint_logged(table.h, table.d, record.buf.data_ptr(),
-                                                              record.buf.numel(), record.cap, record.n_i, record.n_j,
-                                                              g.data_ptr(), out.data_ptr(), ctypes.byref(needed),
-                                                              stream)
+                _native.call("qmbx_apply_within_adjoint_logged", table.h, table.d, record.buf.data_ptr(),
+                             record.buf.numel(), record.cap, record.n_i, record.n_j, record.same, g.data_ptr(),
+                             out.data_ptr(), stream)
             else:
                 want64 = out_dtype == torch.complex128
                 out = torch.empty(record.n_i, dtype=torch.complex128 if want64 else torch.complex64, device=device)
                 o64, o32 = (out.data_ptr(), None) if want64 else (None, out.data_ptr())
-                status = lib.qmbx_apply_within_adjoint_f32c_logged(table.h, table.d, record.buf.data_ptr(),
-                                                                   record.buf.numel(), record.cap, record.n_i,
-                                                                   record.n_j, g.data_ptr(), o64, o32,
-                                                                   ctypes.byref(needed), stream)
-        key = (device.index, record.n_i, record.n_j)
-        if status == _native.QMBX_ERR_WORKSPACE:
-            self._log_caps[key] = int(needed.value * 1.25) + 1024
-            return None
-        _native.check(status)
-        self._log_caps[key] = int(needed.value * 1.25) + 1024
+                _native.call("qmbx_apply_within_adjoint_f32c_logged", table.h, table.d, record.buf.data_ptr(),
+                             record.buf.numel(), record.cap, record.n_i, record.n_j, record.same,
+                             int(record.include_diagonal), g.data_ptr(), o64, o32, stream)
+            count = torch.empty(1, dtype=torch.int64, pin_memory=True)
+            _native.call("qmbx_hitlog_count", record.buf.data_ptr(), count.data_ptr(), stream)
+            done = torch.cuda.Event()
+            done.record(torch.cuda.current_stream(device))
+        record.count = (count, done)
+        state = self._log_caps.get((device.index, record.n_i, record.n_j))
+        if state is not None:
+            state["pending"] = (count, done)
         return out
 
     def apply_within(self, configs_i: torch.Tensor, psi_i: torch.Tensor, configs_j: torch.Tensor) -> torch.Tensor:
@@ -542,10 +563,19 @@ class HamiltonianMatrix:
 class _HitRecord:
     """What a logged forward apply_within found (a device buffer), for its adjoint product."""
 
-    def __init__(self, table: _Table, buf: torch.Tensor, cap: int, n_i: int, n_j: int, dtype: torch.dtype,
-                 include_diagonal: bool):
-        self.table, self.buf, self.cap, self.n_i, self.n_j = table, buf, cap, n_i, n_j
+    def __init__(self, table: _Table, buf: torch.Tensor, cap: int, n_i: int, n_j: int, same: int,
+                 dtype: torch.dtype, include_diagonal: bool):
+        self.table, self.buf, self.cap, self.n_i, self.n_j, self.same = table, buf, cap, n_i, n_j, same
         self.dtype, self.include_diagonal = dtype, include_diagonal
+        self.count = None  # (pinned host int64, event) once the adjoint is queued
+
+    @property
+    def hits(self) -> int | None:
+        """Hits the forward found (waits for the copy queued with the adjoint)."""
+        if self.count is None:
+            return None
+        self.count[1].synchronize()
+        return int(self.count[0][0])
 
 
 class _ApplyWithin(torch.autograd.Function):
@@ -553,8 +583,8 @@ class _ApplyWithin(torch.autograd.Function):
 
     The forward walk records its hits, and the backward replays that record
     (the adjoint needs exactly the (term, row) pairs the forward found); when
-    the record could not hold them all, the backward walks the terms with
-    the adjoint kernel instead.
+    the record could not hold them all, the library walks the adjoint
+    instead, decided on the device, so the backward never waits for it.
     """
 
     @staticmethod
@@ -577,8 +607,9 @@ class _ApplyWithin(torch.autograd.Function):
             return None, None, None, None, None
         g = grad.to(ctx.in_dtype).contiguous()
         want = torch.complex128 if ctx.in_dtype == torch.complex128 else None
-        gi = ctx.ham._adjoint_from_log(ctx.record, g, want) if ctx.record is not None else None
-        if gi is None:
+        if ctx.record is not None:
+            gi = ctx.ham._adjoint_from_log(ctx.record, g, want)
+        else:
             gi = ctx.ham._apply(configs_i, g, configs_j, adjoint=True, out_dtype=want)
         ctx.record = None
         return None, None, gi.to(ctx.in_dtype), None, None

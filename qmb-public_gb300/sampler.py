@@ -12,8 +12,13 @@ methods:
   network again on the sampled rows for psi; here the log amplitudes are
   summed while sampling (the same normalised FP32 terms, summed in FP64 in
   the same site order) and only the phase network runs at the end, which
-  halves the matrix products.  psi is returned detached (callers use it as
-  data: qmb/vmc.py:84, qmb/haar.py:373).
+  halves the matrix products.  The reference drops the candidates whose
+  value is not finite after every site (a host round trip for their
+  count); here they ride along as rows without children and are dropped
+  once at the end.  The rows kept, their order and the uniforms they draw
+  are the same.  psi is
+  returned detached (callers use it as data: qmb/vmc.py:84,
+  qmb/haar.py:373).
 
 The per-site networks are torch ``Linear`` layers (cuBLAS matrix products);
 everything elementwise between them runs in this package's CUDA kernels
@@ -21,8 +26,8 @@ everything elementwise between them runs in this package's CUDA kernels
 and the per-row sum over sites of ``forward`` (one kernel, with its own
 backward for training), and each sampling site's mask, normalisation,
 Gumbel perturbation and conditioning (one kernel) followed by the
-reference's selection (a descending sort, cut at batch_size, non-finite
-values dropped) and one gather of the chosen children.  Inputs must be CUDA
+reference's selection (a descending sort, cut at batch_size) and one
+gather of the chosen children.  Inputs must be CUDA
 tensors; there is no CPU path.
 """
 
@@ -174,6 +179,7 @@ class WaveFunctionElectronUpDown(torch.nn.Module):
         lp = torch.zeros(1, dtype=torch.float32, device=device)
         gp = torch.zeros(1, dtype=torch.float32, device=device)
         la = torch.zeros(1, dtype=torch.float64, device=device)  # log amplitude so far (the forward's sum)
+        bad = torch.zeros(1, dtype=torch.int32, device=device)  # NaN / +inf values of a site (see the kernels)
         with torch.cuda.device(device):
             for i, net in enumerate(self.amplitude):
                 inputs = xf[:, :2 * i]
@@ -183,18 +189,27 @@ class WaveFunctionElectronUpDown(torch.nn.Module):
                     u = torch.rand((n, 4), dtype=torch.float32, device=device)
                 else:
                     u = uniforms(i, n) if callable(uniforms) else uniforms[i]
-                u = u.to(device=device, dtype=torch.float32).contiguous()
+                u = u.to(device=device, dtype=torch.float32)[:n]
+                if u.shape[0] < n:
+                    # a replay gives the reference's rows only; the rows carried past them have no
+                    # children whatever they draw
+                    u = torch.cat([u, torch.full((n - u.shape[0], 4), 0.5, dtype=torch.float32, device=device)])
+                u = u.contiguous()
                 l_all = torch.empty(4 * n, dtype=torch.float32, device=device)
                 t_all = torch.empty(4 * n, dtype=torch.float32, device=device)
                 a_all = torch.empty(4 * n, dtype=torch.float64, device=device)
+                bad.zero_()
                 _native.call("qmbx_sampler_site", n, i, sites, up, down, delta.data_ptr(), counts.data_ptr(),
                              lp.data_ptr(), gp.data_ptr(), u.data_ptr(), l_all.data_ptr(), t_all.data_ptr(),
-                             la.data_ptr(), a_all.data_ptr(), stream)
-                # the batch_size largest conditioned Gumbel values, largest first, then every
-                # value that is not finite dropped -- the reference's own selection
-                # (argsort, then isfinite), NaN included, so that both keep the same rows
-                order = torch.argsort(t_all, descending=True)[:batch_size]
-                index = order[torch.isfinite(t_all[order])].contiguous()
+                             la.data_ptr(), a_all.data_ptr(), bad.data_ptr(), stream)
+                # the batch_size largest conditioned Gumbel values, largest first -- the
+                # reference's own selection (argsort).  The reference then drops the values
+                # that are not finite; here those rows are carried along (the take kernel
+                # marks them, the site kernel gives them no children) and dropped once at the
+                # end, so the row count stays known on the host and the loop never waits for
+                # the device.  NaN and +inf, which the reference's sort puts first, are sorted
+                # after the finite values here, so the kept rows come first, as there
+                index = torch.argsort(t_all, descending=True)[:batch_size].contiguous()
                 m = index.shape[0]
                 occ_n = torch.empty((m, sites), dtype=torch.uint8, device=device)
                 xf_n = torch.zeros((m, 2 * sites), dtype=torch.float32, device=device)
@@ -204,9 +219,14 @@ class WaveFunctionElectronUpDown(torch.nn.Module):
                 la_n = torch.empty(m, dtype=torch.float64, device=device)
                 _native.call("qmbx_sampler_take", m, n, i, sites, index.data_ptr(), occ.data_ptr(), counts.data_ptr(),
                              l_all.data_ptr(), t_all.data_ptr(), occ_n.data_ptr(), xf_n.data_ptr(), counts_n.data_ptr(),
-                             lp_n.data_ptr(), gp_n.data_ptr(), a_all.data_ptr(), la_n.data_ptr(), stream)
+                             lp_n.data_ptr(), gp_n.data_ptr(), a_all.data_ptr(), la_n.data_ptr(), batch_size,
+                             bad.data_ptr(), stream)
                 occ, counts, lp, gp, la, n = occ_n, counts_n, lp_n, gp_n, la_n, m
                 xf = xf_n.to(dtype)
+        # the rows the reference keeps: those whose value is finite (in the same order)
+        keep = torch.isfinite(gp)
+        occ, xf, la = occ[keep], xf[keep], la[keep]
+        n = occ.shape[0]
         # back to the site order of the configurations, then packed
         bits = torch.stack([occ >> 1, occ & 1], dim=-1)
         bits = torch.index_select(bits, 1, self.ordering).reshape(n, self.double_sites)

@@ -90,18 +90,36 @@ def test_autograd_backward_replays_the_log_at_c2(cuda_device):
         assert (gi - walk).abs().max().item() <= tol * scale
 
 
-def test_small_record_falls_back_then_grows(cuda_device):
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
+@pytest.mark.parametrize("case", ["ab_initio_6", "ab_initio_10_complex", "edge_duplicates"])
+def test_small_record_falls_back_then_grows(case, dtype, cuda_device):
+    # a record far too small for the forward's hits: the adjoint is walked instead (decided on the
+    # device), the result is the same, and the next call of this shape records every hit
+    g = golden(case)
+    ham = _ham(g)
+    ham._LOG_FIRST_GUESS = 4
+    ci = torch.from_numpy(g["configs_i"]).to(cuda_device)
+    cj = torch.from_numpy(g["configs_j"]).to(cuda_device)
+    psi = torch.from_numpy(g["psi_i"]).to(cuda_device).to(dtype)
+    gj = torch.randn(cj.shape[0], dtype=torch.complex128, device=cuda_device).to(dtype)
+    walk = ham.apply_within_adjoint(ci, gj, cj)
+    key = (cuda_device.index if cuda_device.index is not None else 0, ci.shape[0], cj.shape[0])
+    tol = 1e-12 if dtype == torch.complex128 else 1e-6
+    for attempt in range(3):
+        p = psi.clone().requires_grad_(True)
+        (gi,) = torch.autograd.grad(ham.apply_within(ci, p, cj), p, grad_outputs=gj)
+        assert (gi - walk).abs().max().item() <= tol * walk.abs().max().item()
+    assert ham._log_caps[key]["cap"] > 4
+
+
+def test_adjoint_of_a_buffer_without_a_log_is_nan(cuda_device):
+    # the device checks the log's header: arguments that do not match it give NaN, not garbage
     g = golden("ab_initio_6")
     ham = _ham(g)
-    ham._LOG_FIRST_GUESS = 4  # far too small for this case
     ci = torch.from_numpy(g["configs_i"]).to(cuda_device)
     cj = torch.from_numpy(g["configs_j"]).to(cuda_device)
     psi = torch.from_numpy(g["psi_i"]).to(cuda_device)
-    gj = torch.randn(cj.shape[0], dtype=torch.complex128, device=cuda_device)
-    walk = ham.apply_within_adjoint(ci, gj, cj)
-    for attempt in range(2):
-        p = psi.clone().requires_grad_(True)
-        (gi,) = torch.autograd.grad(ham.apply_within(ci, p, cj), p, grad_outputs=gj)
-        assert (gi - walk).abs().max().item() <= 1e-12 * walk.abs().max().item()
-    key = (cuda_device.index if cuda_device.index is not None else 0, ci.shape[0], cj.shape[0])
-    assert ham._log_caps[key] > 4
+    y, record = ham._apply(ci, psi, cj, adjoint=False, log=True)
+    record.buf.zero_()
+    got = ham._adjoint_from_log(record, y.new_ones(cj.shape[0]), torch.complex128)
+    assert torch.isnan(got.real).all()
