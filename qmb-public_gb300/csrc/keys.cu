@@ -211,24 +211,31 @@ int exclusive_scan(const int32_t* in, int32_t* out, int64_t n, int* total, int32
 
 constexpr int kSortWarps = 8;
 constexpr int kSortThreads = kSortWarps * 32;
-constexpr int kSortRounds = 16;  // items per lane
-constexpr int kSortTile = kSortThreads * kSortRounds;
+// items per lane: 16 for large sorts; 8 up to kSortSmall items, so that a
+// sort of a few tens of thousands of rows (find_relative's output) spreads
+// over twice the blocks while its per-block digit counts still fit the
+// one-block scan
+constexpr int kSortRounds = 16;
+constexpr int kSortRoundsSmall = 8;
+constexpr int64_t kSortSmall = int64_t(1) << 20;
+
+__host__ __device__ constexpr int sort_rounds(int64_t n) { return n <= kSortSmall ? kSortRoundsSmall : kSortRounds; }
 
 template <int W>
 __device__ __forceinline__ unsigned digit_of(const uint64_t* k, int word, int shift) {
     return (unsigned)(k[word] >> shift) & 0xffu;
 }
 
-// counts[d * nblocks + b] = items of block b with digit d
-template <int W>
+// counts[d * nblocks + b] = items of block b with digit d (R items per lane)
+template <int W, int R>
 __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* __restrict__ keys, int64_t n,
                                                                  int word, int shift, int32_t* __restrict__ counts,
                                                                  int nblocks) {
     __shared__ int32_t hist[256];
     for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d] = 0;
     __syncthreads();
-    int64_t base = (int64_t)blockIdx.x * kSortTile;
-    for (int k = 0; k < kSortRounds; ++k) {
+    int64_t base = (int64_t)blockIdx.x * kSortThreads * R;
+    for (int k = 0; k < R; ++k) {
         int64_t i = base + (int64_t)k * kSortThreads + threadIdx.x;
         if (i < n) {
             unsigned d = (unsigned)(__ldg(keys + i * W + word) >> shift) & 0xffu;
@@ -242,7 +249,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t
 // Scatter with ranks that keep the input order among equal digits: warp w of
 // a block owns items [w*32*R, (w+1)*32*R) of the block's tile, visited round
 // by round (32 consecutive items per round).
-template <int W>
+template <int W, int R>
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint64_t* __restrict__ keys_in,
                                                                     const int32_t* __restrict__ vals_in,
                                                                     uint64_t* __restrict__ keys_out,
@@ -257,12 +264,12 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint6
         s_base[d] = offsets[(int64_t)d * nblocks + blockIdx.x];
     }
     __syncthreads();
-    const int64_t wbase = (int64_t)blockIdx.x * kSortTile + (int64_t)warp * 32 * kSortRounds;
-    unsigned dig[kSortRounds];
-    int32_t rank[kSortRounds];
+    const int64_t wbase = (int64_t)blockIdx.x * kSortThreads * R + (int64_t)warp * 32 * R;
+    unsigned dig[R];
+    int32_t rank[R];
     const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
+    for (int r = 0; r < R; ++r) {
         int64_t i = wbase + (int64_t)r * 32 + lane;
         bool valid = i < n;
         unsigned d = valid ? (unsigned)(__ldg(keys_in + i * W + word) >> shift) & 0xffu : 256u;
@@ -288,7 +295,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint6
     }
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
+    for (int r = 0; r < R; ++r) {
         int64_t i = wbase + (int64_t)r * 32 + lane;
         if (i < n) {
             unsigned d = dig[r];
@@ -302,7 +309,8 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint6
 
 template <int W>
 static int sort_blocks(int64_t n) {
-    int64_t nb = (n + kSortTile - 1) / kSortTile;
+    const int64_t tile = (int64_t)kSortThreads * sort_rounds(n);
+    int64_t nb = (n + tile - 1) / tile;
     return (int)(nb < 1 ? 1 : nb);
 }
 
@@ -338,11 +346,19 @@ int sort_pairs(const uint64_t* keys_in, const int32_t* vals_in, uint64_t* keys_o
         bool to_out = ((n_bytes - 1 - p) & 1) == 0;
         uint64_t* dst_k = to_out ? keys_out : sc.keys;
         int32_t* dst_v = to_out ? vals_out : sc.vals;
-        QMBX_KERNEL(kGroupSort, s, radix_hist_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
+        const bool small = sort_rounds(n) == kSortRoundsSmall;
+        if (small) {
+            QMBX_KERNEL(kGroupSort, s, radix_hist_kernel<W, kSortRoundsSmall><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
+        } else {
+            QMBX_KERNEL(kGroupSort, s, radix_hist_kernel<W, kSortRounds><<<nblocks, kSortThreads, 0, s>>>(src_k, n, word, shift, sc.counts, nblocks));
+        }
         int st = exclusive_scan(sc.counts, sc.counts, (int64_t)256 * nblocks, nullptr, sc.scan, s, kGroupSort);
         if (st != QMBX_OK) return st;
-        QMBX_KERNEL(kGroupSort, s, radix_scatter_kernel<W><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts,
-                                                                 nblocks));
+        if (small) {
+            QMBX_KERNEL(kGroupSort, s, radix_scatter_kernel<W, kSortRoundsSmall><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts, nblocks));
+        } else {
+            QMBX_KERNEL(kGroupSort, s, radix_scatter_kernel<W, kSortRounds><<<nblocks, kSortThreads, 0, s>>>(src_k, src_v, dst_k, dst_v, n, word, shift, sc.counts, nblocks));
+        }
         QMBX_LAUNCH_CHECK("radix sort pass");
         src_k = dst_k;
         src_v = dst_v;

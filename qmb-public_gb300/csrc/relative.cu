@@ -89,8 +89,10 @@ struct RelativeArgs {
     int64_t n_i;
     HashView excl;           // hash set over the unique exclude keys
     PartView off, diag;
-    // pass 1
+    // histogram passes
     unsigned long long* hist;
+    int hist_exact;          // 1: count only records outside the exclusion set (the exact rerun);
+                             // 0: count every record (a threshold estimate: no exclusion lookups)
     // pass 2 (emit_from, the record counter and the overflow flag live in ctl)
     FindCtl* ctl;
     int64_t cap_emit;
@@ -115,6 +117,7 @@ struct RelativeVisitor : VisitorBase {
         float m;
         int64_t row;
         int* hist;
+        int emit_from;  // the emission pass's threshold bucket, read once per row
         double e0re, e0im;
     };
     // the histogram pass counts every record per bucket in shared memory; the
@@ -137,6 +140,7 @@ struct RelativeVisitor : VisitorBase {
         acc.m = __fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py));
         acc.row = row;
         acc.hist = sh;
+        acc.emit_from = EMIT ? a.ctl->emit_from : 0;
         acc.e0re = acc.e0im = 0.0;
     }
     // conj(psi_ex[pos]) * s * coef * psi_row, added to the <psi|H|psi> partial
@@ -165,14 +169,12 @@ struct RelativeVisitor : VisitorBase {
     // stores what identifies the record (term slot and part, parity, row);
     // its exact FP64 weight is formed afterwards by rank_records_kernel, so
     // that the walk issues no FP64 instruction.
-    __device__ __forceinline__ void record(Acc& acc, const Key<W>& img, const PartView& pv, int part, int parity,
-                                           int64_t slot) const {
-        const int b = weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
-        if (!EMIT) {
-            atomicAdd(&acc.hist[b], 1);
-            return;
-        }
-        if (b < a.ctl->emit_from) return;
+    __device__ __forceinline__ int bucket(const Acc& acc, const PartView& pv, int64_t slot) const {
+        return weight_bucket(__fmul_rn(__ldg(pv.norm + slot), acc.m));
+    }
+    // The emission pass's record at or above the threshold whose image is not excluded.
+    __device__ __forceinline__ void emit(const Acc& acc, const Key<W>& img, int part, int parity,
+                                         int64_t slot) const {
         const unsigned long long at = atomicAdd(&a.ctl->n_emit, 1ull);
         if ((int64_t)at >= a.cap_emit) {
             a.ctl->overflow = 1;
@@ -183,26 +185,39 @@ struct RelativeVisitor : VisitorBase {
 #pragma unroll
         for (int q = 0; q < W; ++q) a.emit_keys[at * W + q] = img.w[q];
     }
-    __device__ __forceinline__ bool take(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot,
-                                         int64_t pos, int2&) const {
-        if (pos < 0) record(acc, img, a.off, 0, parity, slot);
-        return false;
+    // One candidate record (term slot of part pv, image img).  The histogram
+    // pass counts it by bucket (outside the exclusion set only when exact, or
+    // for diagonal records).
+    // The emission pass compares its bucket with the threshold first: nearly
+    // every record falls below it and then needs no exclusion lookup; the
+    // PT2 step looks every image up, as the excluded ones make up E0.
+    __device__ __forceinline__ void candidate(Acc& acc, const Key<W>& img, const PartView& pv, int part, int parity,
+                                              int64_t slot) const {
+        if (!EMIT) {
+            // diagonal records (part 1) are always looked up: their image is the row itself,
+            // which the exclusion set usually holds, and their weights are among the largest
+            if ((a.hist_exact || part == 1) && hash_find<W>(lookup, img) >= 0) return;
+            atomicAdd(&acc.hist[bucket(acc, pv, slot)], 1);
+            return;
+        }
+        if (a.e0 != nullptr) {
+            const int64_t pos = hash_find<W>(lookup, img);
+            if (pos >= 0) {
+                add_e0(acc, __ldg(pv.coef + slot), parity, pos);
+                return;
+            }
+            if (bucket(acc, pv, slot) >= acc.emit_from) emit(acc, img, part, parity, slot);
+            return;
+        }
+        if (bucket(acc, pv, slot) < acc.emit_from) return;
+        if (hash_find<W>(lookup, img) >= 0) return;
+        emit(acc, img, part, parity, slot);
     }
     __device__ __forceinline__ void visit(Acc& acc, const Key<W>&, const Key<W>& img, int parity, int64_t slot) const {
-        const int64_t pos = hash_find<W>(lookup, img);
-        if (pos < 0) {
-            record(acc, img, a.off, 0, parity, slot);
-        } else if (EMIT && a.e0 != nullptr) {
-            add_e0(acc, __ldg(a.off.coef + slot), parity, pos);
-        }
+        candidate(acc, img, a.off, 0, parity, slot);
     }
     __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
-        const int64_t pos = hash_find<W>(lookup, c);
-        if (pos < 0) {
-            record(acc, c, a.diag, 1, parity, slot);
-        } else if (EMIT && a.e0 != nullptr) {
-            add_e0(acc, __ldg(a.diag.coef + slot), parity, pos);
-        }
+        candidate(acc, c, a.diag, 1, parity, slot);
     }
     __device__ __forceinline__ void reduce(Acc& acc) const {
         if (EMIT && a.e0 != nullptr) {
@@ -294,45 +309,71 @@ __global__ void sample_rows_kernel(const uint64_t* __restrict__ keys, const doub
     psi_s[j] = psi[r];
 }
 
+// Inclusive scan of v over the 1024 threads of a block in thread order.
+template <class T>
+__device__ __forceinline__ T block_inclusive_scan(T v, T* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const T y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        T w = s_warp[lane];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const T y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    return warp > 0 ? x + s_warp[warp - 1] : x;
+}
+
+constexpr int kChooseThreads = 1024;
+
 // emit_from from the counts of a histogram pass (scaled by `scale`): one
 // bucket below the highest bucket b whose buckets >= b hold at least
 // `target` records (0 when all buckets above 0 hold fewer); then the counts
-// are cleared.  One warp: lane l sums the 128 buckets [4096 - 128(l + 1),
-// 4096 - 128 l), a suffix scan over the lanes finds the lane where the
-// running count reaches the target, and that lane walks its buckets.
-__global__ void choose_emit_kernel(unsigned long long* __restrict__ hist, double scale, double target,
-                                   FindCtl* __restrict__ ctl) {
-    const int lane = threadIdx.x;
-    constexpr int kPer = kBuckets / 32;
-    const int hi = kBuckets - kPer * lane;  // lane covers buckets [hi - kPer, hi)
-    double mine = 0.0;
-    for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) mine += scale * (double)hist[b];
-    // inclusive scan from the top lanes down (lane 0 holds the highest buckets)
-    double run = mine;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, run, d);
-        if (lane >= d) run += y;
-    }
-    const unsigned crossed = __ballot_sync(0xffffffffu, run >= target);
-    int b_k = 0;
-    if (crossed) {
-        const int first = __ffs(crossed) - 1;
-        if (lane == first) {
-            double above = run - mine;
-            for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) {
-                above += scale * (double)hist[b];
-                if (above >= target) {
-                    b_k = b;
-                    break;
-                }
+// are cleared.  One block of 1024 threads: thread t sums the 4 buckets
+// [4096 - 4(t + 1), 4096 - 4t), a scan over the threads (highest buckets
+// first) finds the one thread where the running count reaches the target,
+// and that thread walks its buckets.
+__global__ void __launch_bounds__(kChooseThreads) choose_emit_kernel(unsigned long long* __restrict__ hist,
+                                                                     double scale, double target,
+                                                                     FindCtl* __restrict__ ctl) {
+    __shared__ unsigned long long s_warp[32];
+    __shared__ int s_found;
+    constexpr int kPer = kBuckets / kChooseThreads;
+    const int t = threadIdx.x;
+    const int hi = kBuckets - kPer * t;  // thread t covers buckets [hi - kPer, hi)
+    if (t == 0) s_found = 0;
+    // integer counts, scaled only where compared: the running count is exact and monotone, so
+    // exactly one thread sees it cross the target
+    unsigned long long mine = 0;
+    for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) mine += hist[b];
+    const unsigned long long run = block_inclusive_scan(mine, s_warp);
+    if (scale * (double)run >= target && scale * (double)(run - mine) < target) {
+        // the one thread whose buckets reach the target
+        unsigned long long above = run - mine;
+        int b_k = 0;
+        for (int b = hi - 1; b >= hi - kPer && b >= 1; --b) {
+            above += hist[b];
+            if (scale * (double)above >= target) {
+                b_k = b;
+                break;
             }
         }
-        b_k = __shfl_sync(0xffffffffu, b_k, first);
+        ctl->emit_from = b_k > 1 ? b_k - 1 : 0;
+        s_found = 1;
     }
-    __syncwarp();
-    for (int b = lane; b < kBuckets; b += 32) hist[b] = 0;
-    if (lane == 0) ctl->emit_from = b_k > 1 ? b_k - 1 : 0;
+    __syncthreads();
+    if (t == 0 && !s_found) ctl->emit_from = 0;
+    for (int b = t; b < kBuckets; b += kChooseThreads) hist[b] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -405,31 +446,24 @@ __global__ void select_hist_kernel(const uint64_t* __restrict__ rank, int64_t n,
 }
 
 // One warp: the digit where the remaining count is reached; clears the bins.
-__global__ void select_choose_kernel(int key_bits_total, FindCtl* __restrict__ ctl, unsigned int* __restrict__ bins) {
-    const int lane = threadIdx.x;
+__global__ void __launch_bounds__(kChooseThreads) select_choose_kernel(int key_bits_total, FindCtl* __restrict__ ctl,
+                                                                       unsigned int* __restrict__ bins) {
+    __shared__ long long s_warp[32];
     if (ctl->sel_done) return;
+    const int t = threadIdx.x;
     const int fixed = ctl->sel_bits;
     const int cnt = key_bits_total - fixed < kSelectBits ? key_bits_total - fixed : kSelectBits;
     const int nbins = 1 << cnt;
-    const int per = (nbins + 31) / 32;
-    const int lo = lane * per;
+    const int per = (nbins + kChooseThreads - 1) / kChooseThreads;
+    const int lo = t * per;
     long long mine = 0;
     for (int b = lo; b < lo + per && b < nbins; ++b) mine += bins[b];
-    long long run = mine;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const long long y = __shfl_up_sync(0xffffffffu, run, d);
-        if (lane >= d) run += y;
-    }
+    const long long run = block_inclusive_scan(mine, s_warp);
     const long long need = ctl->sel_need;
-    const unsigned crossed = __ballot_sync(0xffffffffu, run >= need);
-    // crossed is never empty: the records under the prefix hold at least `need`
-    const int first = crossed ? __ffs(crossed) - 1 : 31;
-    int digit = 0;
-    long long below = 0, at = 0;
-    if (lane == first) {
+    // the records under the prefix hold at least `need`: exactly one thread's bins reach it
+    if (run >= need && run - mine < need) {
         long long acc = run - mine;
-        digit = lo + per - 1 < nbins - 1 ? lo + per - 1 : nbins - 1;
+        int digit = lo + per - 1 < nbins - 1 ? lo + per - 1 : nbins - 1;
         for (int b = lo; b < lo + per && b < nbins; ++b) {
             if (acc + (long long)bins[b] >= need) {
                 digit = b;
@@ -437,34 +471,28 @@ __global__ void select_choose_kernel(int key_bits_total, FindCtl* __restrict__ c
             }
             acc += bins[b];
         }
-        below = acc;
-        at = bins[digit];
-    }
-    digit = __shfl_sync(0xffffffffu, digit, first);
-    below = __shfl_sync(0xffffffffu, below, first);
-    at = __shfl_sync(0xffffffffu, at, first);
-    __syncwarp();
-    for (int b = lane; b < kSelectBins; b += 32) bins[b] = 0;
-    if (lane == 0) {
+        const long long below = acc, at = bins[digit];
         // place the digit below the fixed bits
-        const int from = fixed;
         uint64_t p0 = ctl->sel_p0, p1 = ctl->sel_p1;
         const uint64_t d = (uint64_t)digit;
-        if (from + cnt <= 64) {
-            p0 |= d << (64 - from - cnt);
-        } else if (from >= 64) {
-            p1 |= d << (128 - from - cnt);
+        if (fixed + cnt <= 64) {
+            p0 |= d << (64 - fixed - cnt);
+        } else if (fixed >= 64) {
+            p1 |= d << (128 - fixed - cnt);
         } else {
-            const int lo_bits = from + cnt - 64;
+            const int lo_bits = fixed + cnt - 64;
             p0 |= d >> lo_bits;
             p1 |= d << (64 - lo_bits);
         }
         ctl->sel_p0 = p0;
         ctl->sel_p1 = p1;
-        ctl->sel_bits = fixed + cnt;
         ctl->sel_need = need - below;
         if (at == need - below || fixed + cnt >= key_bits_total) ctl->sel_done = 1;
     }
+    __syncthreads();
+    // every thread has read ctl->sel_bits before it moves on (the fixed-bit count of this level)
+    if (t == 0) ctl->sel_bits = fixed + cnt;
+    for (int b = t; b < kSelectBins; b += kChooseThreads) bins[b] = 0;
 }
 
 // Keys of the accepted records (rank prefix at most the chosen prefix), in no particular order.
@@ -596,6 +624,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.off = part_view(a.table_host, a.table_dev, QMBX_PART_FWD);
     r.diag = part_view(a.table_host, a.table_dev, QMBX_PART_DIAG);
     r.hist = L.hist;
+    r.hist_exact = 1;
     r.ctl = L.ctl;
     r.cap_emit = cap;
     r.emit_rank = L.emit_rank;
@@ -619,14 +648,17 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         RelativeArgs rs = r;
         rs.psi = L.psi_s;
         rs.n_i = n_s;
+        rs.hist_exact = 0;  // an estimate: every record counted, no exclusion lookups
         if ((st = launch_relative<W, false>(rs, L.keys_s, n_s, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
         // aim at about twice k records above the chosen bucket, one more bucket of slack
-        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, 32, 0, s>>>(L.hist, (double)a.n_i / (double)n_s, 2.0 * (double)k, L.ctl));
+        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, kChooseThreads, 0, s>>>(L.hist, (double)a.n_i / (double)n_s, 2.0 * (double)k, L.ctl));
     } else {
-        if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
+        RelativeArgs r1 = r;
+        r1.hist_exact = 0;
+        if ((st = launch_relative<W, false>(r1, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
-        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, 32, 0, s>>>(L.hist, 1.0, (double)k, L.ctl));
+        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, kChooseThreads, 0, s>>>(L.hist, 1.0, (double)k, L.ctl));
     }
     QMBX_LAUNCH_CHECK("choose_emit_kernel");
 
@@ -654,7 +686,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
         if ((st = launch_relative<W, false>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
         QMBX_CUDA_TRY(cudaMemsetAsync(L.ctl, 0, sizeof(FindCtl), s));
-        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, 32, 0, s>>>(L.hist, 1.0, (double)k, L.ctl));
+        QMBX_KERNEL(kGroupSelect, s, choose_emit_kernel<<<1, kChooseThreads, 0, s>>>(L.hist, 1.0, (double)k, L.ctl));
         QMBX_LAUNCH_CHECK("choose_emit_kernel");
     }
     g_find_stats.records = (int64_t)ctl.n_emit;
@@ -676,7 +708,7 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     const unsigned sel_grid = grid_for(e, kThreads) < 2u * 152u ? grid_for(e, kThreads) : 2u * 152u;
     for (int level = 0; level < levels; ++level) {
         QMBX_KERNEL(kGroupSelect, s, select_hist_kernel<<<sel_grid, kThreads, 0, s>>>(L.emit_rank, e, key_bits_total, L.ctl, L.bins));
-        QMBX_KERNEL(kGroupSelect, s, select_choose_kernel<<<1, 32, 0, s>>>(key_bits_total, L.ctl, L.bins));
+        QMBX_KERNEL(kGroupSelect, s, select_choose_kernel<<<1, kChooseThreads, 0, s>>>(key_bits_total, L.ctl, L.bins));
     }
     QMBX_KERNEL(kGroupSelect, s, select_compact_kernel<W><<<grid_for(e, kThreads), kThreads, 0, s>>>(L.emit_rank, L.emit_keys, e, L.ctl, L.sel_keys));
     QMBX_LAUNCH_CHECK("find_relative selection");

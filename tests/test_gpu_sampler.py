@@ -172,3 +172,50 @@ def test_sampling_run_matches_the_restatement_end_to_end(cuda_device):
         assert torch.allclose(net(common), oracle_sampler.forward(params, 20, 6, 6, common), rtol=1e-5, atol=0)
         # psi summed while sampling equals the network's forward on the sampled rows
         assert torch.allclose(psi, net(configs), rtol=1e-5, atol=0)
+
+
+def test_site_kernel_sorts_nan_and_inf_values_after_the_finite_ones(cuda_device):
+    # a row whose children's perturbed log probabilities all lie below -88 has exp(-Z) = inf and
+    # conditioned values NaN; the reference's descending sort puts those first and then drops them.
+    # With a counter the site kernel writes them as -FLT_MAX (after the finite values) and counts
+    # them, and the take kernel drops the places they took at the top of the reference's sort.
+    native = __import__("importlib").import_module("qmb-public_gb300._native")
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    sites, up, down, n, batch = 4, 2, 2, 3, 5
+    delta = torch.zeros((n, 4), dtype=torch.float32, device=cuda_device)
+    counts = torch.zeros((n, 2), dtype=torch.int32, device=cuda_device)
+    lp = torch.tensor([0.0, -400.0, -1.0], dtype=torch.float32, device=cuda_device)  # row 1: far below -88
+    gp = torch.tensor([0.0, -0.5, -0.25], dtype=torch.float32, device=cuda_device)
+    u = torch.tensor([[0.1, 0.3, 0.5, 0.7]] * n, dtype=torch.float32, device=cuda_device)  # no ties
+    l_all = torch.empty(4 * n, dtype=torch.float32, device=cuda_device)
+    t_all = torch.empty(4 * n, dtype=torch.float32, device=cuda_device)
+    raw = torch.empty(4 * n, dtype=torch.float32, device=cuda_device)
+    native.call("qmbx_sampler_site", n, 0, sites, up, down, delta.data_ptr(), counts.data_ptr(), lp.data_ptr(),
+                gp.data_ptr(), u.data_ptr(), l_all.data_ptr(), raw.data_ptr(), None, None, None, stream)
+    bad = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    native.call("qmbx_sampler_site", n, 0, sites, up, down, delta.data_ptr(), counts.data_ptr(), lp.data_ptr(),
+                gp.data_ptr(), u.data_ptr(), l_all.data_ptr(), t_all.data_ptr(), None, None, bad.data_ptr(), stream)
+    torch.cuda.synchronize(cuda_device)
+    not_finite = ~torch.isfinite(raw) & (raw != -torch.inf)  # NaN or +inf
+    k = int(not_finite.sum())
+    assert k > 0 and int(bad.item()) == k
+    assert torch.equal(t_all[not_finite], torch.full((k,), torch.finfo(torch.float32).min, device=cuda_device))
+    assert torch.equal(t_all[~not_finite], raw[~not_finite])
+    # the reference keeps the finite values among the first `batch` of its descending sort (NaN first)
+    ref_order = torch.argsort(torch.where(torch.isnan(raw), torch.inf, raw), descending=True)[:batch]
+    kept_ref = [int(i) for i in ref_order if torch.isfinite(raw[i])]
+    index = torch.argsort(t_all, descending=True)[:batch].contiguous()
+    m = index.shape[0]
+    occ = torch.zeros((n, sites), dtype=torch.uint8, device=cuda_device)
+    out = dict(occ=torch.empty((m, sites), dtype=torch.uint8, device=cuda_device),
+               xf=torch.zeros((m, 2 * sites), dtype=torch.float32, device=cuda_device),
+               counts=torch.empty((m, 2), dtype=torch.int32, device=cuda_device),
+               lp=torch.empty(m, dtype=torch.float32, device=cuda_device),
+               gp=torch.empty(m, dtype=torch.float32, device=cuda_device))
+    native.call("qmbx_sampler_take", m, n, 0, sites, index.data_ptr(), occ.data_ptr(), counts.data_ptr(),
+                l_all.data_ptr(), t_all.data_ptr(), out["occ"].data_ptr(), out["xf"].data_ptr(),
+                out["counts"].data_ptr(), out["lp"].data_ptr(), out["gp"].data_ptr(), None, None, batch,
+                bad.data_ptr(), stream)
+    torch.cuda.synchronize(cuda_device)
+    kept = [int(index[j]) for j in range(m) if torch.isfinite(out["gp"][j])]
+    assert kept == kept_ref
