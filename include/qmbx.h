@@ -303,11 +303,11 @@ int qmbx_find_relative_stats(int64_t stats[6]);
  *   energies[0] = E0 = Re<psi|H|psi> / <psi|psi> over configs (n distinct rows),
  *   other = find_relative(configs, psi, count_selected, configs),
  *   energies[1] = E2 = sum over other of |(H psi)_j|^2 / <psi|psi> / (E0 - Re H_jj),
- * *n_other = the number of rows of other.  E0 is summed by find_relative's
- * emission pass (its exclusion set is configs), so the step walks the terms
- * once fewer than the composition.  count_selected >= 1.  Synchronises the
- * stream.  Workspace as for qmbx_find_relative: on QMBX_ERR_WORKSPACE
- * *workspace_needed holds the size to retry with.
+ * *n_other = the number of rows of other.  One apply_within from configs
+ * onto configs and other together gives E0's H psi and other's, so the step
+ * walks the terms once fewer than the composition.  count_selected >= 1.
+ * Synchronises the stream.  Workspace as for qmbx_find_relative: on
+ * QMBX_ERR_WORKSPACE *workspace_needed holds the size to retry with.
  * ------------------------------------------------------------------------- */
 
 int qmbx_pt2_workspace(const void* table_host, int64_t n, int64_t count_selected, uint64_t* bytes);

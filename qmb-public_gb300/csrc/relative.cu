@@ -99,13 +99,6 @@ struct RelativeArgs {
     uint64_t* emit_rank;     // [cap][2]: (slot | part << 62 | parity << 63, row) from the walk;
                              // (~weight bits, ~order) after rank_records_kernel
     uint64_t* emit_keys;     // [cap][W]
-    // when non-NULL (the PT2 step, whose exclusion set is configs_i itself):
-    // the emission pass also sums conj(psi_ex[j]) * s * coef * psi[i] over
-    // the records whose image j IS excluded, i.e. the numerator of
-    // <psi|H|psi>, into e0[blockIdx.x % e0_slots]
-    double2* e0;
-    const double2* psi_ex;
-    int e0_slots;
 };
 
 template <int W, bool EMIT>
@@ -118,7 +111,6 @@ struct RelativeVisitor : VisitorBase {
         int64_t row;
         int* hist;
         int emit_from;  // the emission pass's threshold bucket, read once per row
-        double e0re, e0im;
     };
     // the histogram pass counts every record per bucket in shared memory; the
     // emission pass counts only what it emits (its record counter)
@@ -141,27 +133,6 @@ struct RelativeVisitor : VisitorBase {
         acc.row = row;
         acc.hist = sh;
         acc.emit_from = EMIT ? a.ctl->emit_from : 0;
-        acc.e0re = acc.e0im = 0.0;
-    }
-    // conj(psi_ex[pos]) * s * coef * psi_row, added to the <psi|H|psi> partial
-    __device__ __forceinline__ void add_e0(Acc& acc, double2 cf, int parity, int64_t pos) const {
-        const double2 q = __ldg(a.psi_ex + pos);
-        double tr = cf.x * acc.p.x - cf.y * acc.p.y;
-        double ti = cf.x * acc.p.y + cf.y * acc.p.x;
-        if (parity) {
-            tr = -tr;
-            ti = -ti;
-        }
-        acc.e0re += q.x * tr + q.y * ti;
-        acc.e0im += q.x * ti - q.y * tr;
-    }
-    __device__ __forceinline__ void flush_e0(Acc& acc) const {
-        if (acc.e0re != 0.0 || acc.e0im != 0.0) {
-            double2* slot = a.e0 + (blockIdx.x % a.e0_slots);
-            atomicAdd(&slot->x, acc.e0re);
-            atomicAdd(&slot->y, acc.e0im);
-        }
-        acc.e0re = acc.e0im = 0.0;
     }
     static constexpr bool kProbe = true;
     HashView lookup;  // the exclusion set
@@ -187,10 +158,9 @@ struct RelativeVisitor : VisitorBase {
     }
     // One candidate record (term slot of part pv, image img).  The histogram
     // pass counts it by bucket (outside the exclusion set only when exact, or
-    // for diagonal records).
-    // The emission pass compares its bucket with the threshold first: nearly
-    // every record falls below it and then needs no exclusion lookup; the
-    // PT2 step looks every image up, as the excluded ones make up E0.
+    // for diagonal records).  The emission pass compares its bucket with the
+    // threshold first: nearly every record falls below it and then needs no
+    // exclusion lookup.
     __device__ __forceinline__ void candidate(Acc& acc, const Key<W>& img, const PartView& pv, int part, int parity,
                                               int64_t slot) const {
         if (!EMIT) {
@@ -198,15 +168,6 @@ struct RelativeVisitor : VisitorBase {
             // which the exclusion set usually holds, and their weights are among the largest
             if ((a.hist_exact || part == 1) && hash_find<W>(lookup, img) >= 0) return;
             atomicAdd(&acc.hist[bucket(acc, pv, slot)], 1);
-            return;
-        }
-        if (a.e0 != nullptr) {
-            const int64_t pos = hash_find<W>(lookup, img);
-            if (pos >= 0) {
-                add_e0(acc, __ldg(pv.coef + slot), parity, pos);
-                return;
-            }
-            if (bucket(acc, pv, slot) >= acc.emit_from) emit(acc, img, part, parity, slot);
             return;
         }
         if (bucket(acc, pv, slot) < acc.emit_from) return;
@@ -219,20 +180,8 @@ struct RelativeVisitor : VisitorBase {
     __device__ __forceinline__ void visit_diag(Acc& acc, const Key<W>& c, int parity, int64_t slot) const {
         candidate(acc, c, a.diag, 1, parity, slot);
     }
-    __device__ __forceinline__ void reduce(Acc& acc) const {
-        if (EMIT && a.e0 != nullptr) {
-            acc.e0re = warp_sum(acc.e0re);
-            acc.e0im = warp_sum(acc.e0im);
-        }
-    }
-    // grouped walks: lane 0 after reduce(); tiled walks: every thread
-    __device__ __forceinline__ void finish(Acc& acc, int64_t, const Key<W>&) const {
-        if (EMIT && a.e0 != nullptr) flush_e0(acc);
-    }
-    // pivot-major walks: one (row, group) partial
-    __device__ __forceinline__ void flush(Acc& acc, int64_t, const Key<W>&) const {
-        if (EMIT && a.e0 != nullptr) flush_e0(acc);
-    }
+    __device__ __forceinline__ void reduce(Acc&) const {}
+    __device__ __forceinline__ void finish(Acc&, int64_t, const Key<W>&) const {}
 };
 
 template <int W, bool EMIT>
@@ -533,8 +482,6 @@ struct FindArgs {
     int64_t n_ex;
     uint8_t* out;
     int64_t* n_out;
-    double2* e0;        // PT2 only (see RelativeArgs::e0); NULL otherwise
-    int e0_slots;
 };
 
 // Workspace layout: fixed part (exclude set, packed rows, histogram, control
@@ -629,9 +576,6 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     r.cap_emit = cap;
     r.emit_rank = L.emit_rank;
     r.emit_keys = L.emit_keys;
-    r.e0 = a.e0;
-    r.psi_ex = r.psi;
-    r.e0_slots = a.e0_slots;
     auto need_bytes = [&](unsigned long long records) {
         Arena want(nullptr, 0);
         take_find<W>(want, a.n_i, k, a.n_ex, (int64_t)records);
@@ -669,7 +613,6 @@ int find_impl(const FindArgs& a, void* workspace, uint64_t workspace_bytes, uint
     // pass (never seen on the benchmark shapes; the tests drive it).
     FindCtl ctl{};
     for (int attempt = 0;; ++attempt) {
-        if (a.e0 != nullptr) QMBX_CUDA_TRY(cudaMemsetAsync(a.e0, 0, (size_t)a.e0_slots * sizeof(double2), s));
         if ((st = launch_relative<W, true>(r, L.keys_i, a.n_i, s)) != QMBX_OK) return st;
         ++g_find_stats.walks;
         QMBX_CUDA_TRY(cudaMemcpyAsync(&ctl, L.ctl, sizeof(FindCtl), cudaMemcpyDeviceToHost, s));
@@ -916,8 +859,7 @@ extern "C" int qmbx_find_relative(const void* table_host, const void* table_dev,
     if (count_selected > 0 && out == nullptr) return fail(QMBX_ERR_ARGUMENT, "out must not be NULL");
     if ((st = check_ws(workspace)) != QMBX_OK) return st;
     if (workspace == nullptr) workspace_bytes = 0;
-    FindArgs a{table_host, table_dev, configs_i, psi_i, n_i, count_selected, configs_exclude, n_exclude, out, n_out,
-               nullptr, 0};
+    FindArgs a{table_host, table_dev, configs_i, psi_i, n_i, count_selected, configs_exclude, n_exclude, out, n_out};
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     switch (header_of(table_host)->n_words) {
         case 1: return find_impl<1>(a, workspace, workspace_bytes, workspace_needed, s);
@@ -985,19 +927,17 @@ extern "C" int qmbx_single_relative(const void* table_host, const void* table_de
 //   E0 = Re<psi|H|psi> / <psi|psi> over configs,
 //   other = find_relative(configs, psi, count_selected, configs),
 //   E2 = sum_j |(H psi)_j|^2 / <psi|psi> / (E0 - Re H_jj) over other.
-// The reference walks the terms four times (apply_within for E0,
-// find_relative, apply_within onto other, diagonal_term).  Here E0 comes out
-// of find_relative's emission pass: its exclusion set is configs itself, so
-// the records it skips are exactly the terms of <psi|H|psi>; the remaining
-// walks are find_relative's sampled threshold pass, the scatter of H psi
-// onto the selected rows and the diagonal terms of those rows, all on the
-// device with E0 never leaving it.
+// The reference walks the terms four times: apply_within for E0,
+// find_relative, apply_within onto other, and diagonal_term.  Here
+// find_relative runs as on its own, and one apply_within from configs onto
+// configs and the selected rows together gives both E0's H psi and the
+// selected rows' (configs and the selected rows are disjoint).  The
+// selected rows' diagonal terms follow.  E0 never leaves the device.
 // ---------------------------------------------------------------------------
 
 namespace qmbx {
 namespace {
 
-constexpr int kE0Slots = 1024;
 constexpr int kPt2Blocks = 1024;
 
 // Deterministic block sum of one double per thread (blockDim.x a multiple of 32, at most 1024).
@@ -1012,14 +952,14 @@ __device__ __forceinline__ double block_sum(double x, double* s_warp) {
     return t;  // valid in warp 0
 }
 
-// sums[0] = E0 = Re(sum of the slots) / norm, sums[1] = norm = <psi|psi>
-__global__ void pt2_e0_kernel(const double2* __restrict__ slots, int n_slots, const double2* __restrict__ psi,
-                              int64_t n, double* __restrict__ sums) {
+// sums[0] = E0 = Re<psi|H psi> / norm over the n configs, sums[1] = norm = <psi|psi>
+__global__ void pt2_e0_kernel(const double2* __restrict__ psi, const double2* __restrict__ hpsi, int64_t n,
+                              double* __restrict__ sums) {
     __shared__ double s_warp[32];
     double num = 0.0, norm = 0.0;
-    for (int k = threadIdx.x; k < n_slots; k += blockDim.x) num += slots[k].x;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const double2 p = psi[i];
+        const double2 p = psi[i], h = hpsi[i];
+        num += p.x * h.x + p.y * h.y;
         norm += p.x * p.x + p.y * p.y;
     }
     num = block_sum(num, s_warp);
@@ -1053,21 +993,19 @@ __global__ void pt2_sum_kernel(const double* __restrict__ partials, int nb, doub
 }
 
 struct Pt2Layout {
-    uint8_t* rows;
-    double2* hpsi;
-    double2* diag;
-    double2* slots;
+    uint8_t* rows;  // configs (n rows), then the selected rows (at most k)
+    double2* hpsi;  // H psi on the same rows
+    double2* diag;  // the selected rows' diagonal terms
     double* sums;
     double* partials;
 };
 
-Pt2Layout take_pt2(Arena& ws, int64_t k, int nq) {
+Pt2Layout take_pt2(Arena& ws, int64_t n, int64_t k, int nq) {
     Pt2Layout L;
     const uint64_t kk = (uint64_t)(k > 0 ? k : 1);
-    L.rows = ws.take<uint8_t>(kk * (uint64_t)nq);
-    L.hpsi = ws.take<double2>(kk);
+    L.rows = ws.take<uint8_t>((uint64_t)(n + kk) * (uint64_t)nq);
+    L.hpsi = ws.take<double2>((uint64_t)n + kk);
     L.diag = ws.take<double2>(kk);
-    L.slots = ws.take<double2>(kE0Slots);
     L.sums = ws.take<double>(4);
     L.partials = ws.take<double>(kPt2Blocks);
     return L;
@@ -1082,11 +1020,11 @@ extern "C" int qmbx_pt2_workspace(const void* table_host, int64_t n, int64_t cou
     if (h == nullptr || h->magic != QMBX_MAGIC) return fail(QMBX_ERR_ARGUMENT, "not a compiled qmbx table");
     if (bytes == nullptr) return fail(QMBX_ERR_ARGUMENT, "bytes must not be NULL");
     Arena fixed(nullptr, 0);
-    take_pt2(fixed, count_selected, h->n_qubytes);
+    take_pt2(fixed, n, count_selected, h->n_qubytes);
     uint64_t find = 0, apply = 0;
     int st = qmbx_find_relative_workspace(table_host, n, count_selected, n, &find);
     if (st != QMBX_OK) return st;
-    if ((st = qmbx_apply_within_workspace(table_host, n, count_selected, &apply)) != QMBX_OK) return st;
+    if ((st = qmbx_apply_within_workspace(table_host, n, n + count_selected, &apply)) != QMBX_OK) return st;
     *bytes = fixed.used + (find > apply ? find : apply);
     return QMBX_OK;
 }
@@ -1106,7 +1044,7 @@ extern "C" int qmbx_pt2(const void* table_host, const void* table_dev, const uin
     if ((st = check_ws(workspace)) != QMBX_OK) return st;
     const qmbx_table_header* h = header_of(table_host);
     Arena fixed(workspace, workspace == nullptr ? 0 : workspace_bytes);
-    Pt2Layout L = take_pt2(fixed, count_selected, h->n_qubytes);
+    Pt2Layout L = take_pt2(fixed, n, count_selected, h->n_qubytes);
     if (workspace == nullptr || !fixed.fits()) {
         uint64_t want = 0;
         qmbx_pt2_workspace(table_host, n, count_selected, &want);
@@ -1117,8 +1055,10 @@ extern "C" int qmbx_pt2(const void* table_host, const void* table_dev, const uin
     const uint64_t scratch_bytes = workspace_bytes - fixed.used;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     *n_other = 0;
-    // find_relative with the E0 numerator summed by its emission pass
-    FindArgs a{table_host, table_dev, configs, psi, n, count_selected, configs, n, L.rows, n_other, L.slots, kE0Slots};
+    const int nq = h->n_qubytes;
+    // the configs first, the selected rows after them
+    QMBX_CUDA_TRY(cudaMemcpyAsync(L.rows, configs, (size_t)n * nq, cudaMemcpyDeviceToDevice, s));
+    FindArgs a{table_host, table_dev, configs, psi, n, count_selected, configs, n, L.rows + (size_t)n * nq, n_other};
     uint64_t find_needed = 0;
     switch (h->n_words) {
         case 1: st = find_impl<1>(a, scratch, scratch_bytes, &find_needed, s); break;
@@ -1130,24 +1070,26 @@ extern "C" int qmbx_pt2(const void* table_host, const void* table_dev, const uin
     if (st == QMBX_ERR_WORKSPACE && workspace_needed) *workspace_needed = fixed.used + find_needed;
     if (st != QMBX_OK) return st;
     const int64_t m = *n_other;
-    QMBX_KERNEL(kGroupSelect, s, pt2_e0_kernel<<<1, 1024, 0, s>>>(L.slots, kE0Slots, reinterpret_cast<const double2*>(psi), n, L.sums));
+    // H psi onto the configs (for E0) and the selected rows at once
+    if ((st = qmbx_apply_within(table_host, table_dev, configs, psi, n, L.rows, n + m, 0,
+                                reinterpret_cast<double*>(L.hpsi), scratch, scratch_bytes, stream)) != QMBX_OK) {
+        if (st == QMBX_ERR_WORKSPACE && workspace_needed) {
+            uint64_t apply = 0;
+            qmbx_apply_within_workspace(table_host, n, n + m, &apply);
+            *workspace_needed = fixed.used + apply;
+        }
+        return st;
+    }
+    QMBX_KERNEL(kGroupSelect, s, pt2_e0_kernel<<<1, 1024, 0, s>>>(reinterpret_cast<const double2*>(psi), L.hpsi, n, L.sums));
     QMBX_LAUNCH_CHECK("pt2_e0_kernel");
     if (m > 0) {
-        // H psi onto the selected rows, and their diagonal terms
-        if ((st = qmbx_apply_within(table_host, table_dev, configs, psi, n, L.rows, m, 0,
-                                    reinterpret_cast<double*>(L.hpsi), scratch, scratch_bytes, stream)) != QMBX_OK) {
-            if (st == QMBX_ERR_WORKSPACE && workspace_needed) {
-                uint64_t apply = 0;
-                qmbx_apply_within_workspace(table_host, n, m, &apply);
-                *workspace_needed = fixed.used + apply;
-            }
-            return st;
-        }
-        if ((st = qmbx_diagonal_term(table_host, table_dev, L.rows, m, reinterpret_cast<double*>(L.diag), stream)) != QMBX_OK) {
+        // the selected rows' diagonal terms
+        if ((st = qmbx_diagonal_term(table_host, table_dev, L.rows + (size_t)n * nq, m, reinterpret_cast<double*>(L.diag),
+                                     stream)) != QMBX_OK) {
             return st;
         }
         const unsigned nb = grid_for(m, 256) < (unsigned)kPt2Blocks ? grid_for(m, 256) : (unsigned)kPt2Blocks;
-        QMBX_KERNEL(kGroupSelect, s, pt2_terms_kernel<<<nb, 256, 0, s>>>(L.hpsi, L.diag, m, L.sums, L.partials));
+        QMBX_KERNEL(kGroupSelect, s, pt2_terms_kernel<<<nb, 256, 0, s>>>(L.hpsi + n, L.diag, m, L.sums, L.partials));
         QMBX_KERNEL(kGroupSelect, s, pt2_sum_kernel<<<1, 1024, 0, s>>>(L.partials, (int)nb, L.sums));
         QMBX_LAUNCH_CHECK("pt2 sums");
     } else {

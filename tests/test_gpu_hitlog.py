@@ -90,11 +90,15 @@ def test_autograd_backward_replays_the_log_at_c2(cuda_device):
         assert (gi - walk).abs().max().item() <= tol * scale
 
 
+@pytest.mark.parametrize("walk", ["auto", "tiled", "pivot"])
 @pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
 @pytest.mark.parametrize("case", ["ab_initio_6", "ab_initio_10_complex", "edge_duplicates"])
-def test_small_record_falls_back_then_grows(case, dtype, cuda_device):
+def test_small_record_falls_back_then_grows(case, dtype, walk, cuda_device, monkeypatch):
     # a record far too small for the forward's hits: the adjoint is walked instead (decided on the
-    # device), the result is the same, and the next call of this shape records every hit
+    # device, over the row sets the forward left in the log), the result is the same, and the next
+    # call of this shape records every hit
+    if walk != "auto":
+        monkeypatch.setenv("QMBX_WALK", walk)
     g = golden(case)
     ham = _ham(g)
     ham._LOG_FIRST_GUESS = 4
@@ -123,3 +127,24 @@ def test_adjoint_of_a_buffer_without_a_log_is_nan(cuda_device):
     record.buf.zero_()
     got = ham._adjoint_from_log(record, y.new_ones(cj.shape[0]), torch.complex128)
     assert torch.isnan(got.real).all()
+
+
+@pytest.mark.parametrize("dtype", [torch.complex128, torch.complex64])
+def test_backward_on_the_same_rows(dtype, cuda_device):
+    # configs_i and configs_j the same tensor (one row set; the forward gathers): the backward
+    # through the log equals the oracle's adjoint
+    g = golden("ab_initio_10_complex")
+    rows = np.unique(np.concatenate([g["configs_i"], g["configs_j"]]), axis=0)
+    ham = _ham(g)
+    rng = np.random.default_rng(5)
+    psi = rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])
+    gj = rng.standard_normal(rows.shape[0]) + 1j * rng.standard_normal(rows.shape[0])
+    c = torch.from_numpy(rows).to(cuda_device)
+    p = torch.from_numpy(psi).to(cuda_device).to(dtype).requires_grad_(True)
+    gt = torch.from_numpy(gj).to(cuda_device).to(dtype)
+    (gi,) = torch.autograd.grad(ham.apply_within(c, p, c), p, grad_outputs=gt)
+    g_used = gj if dtype == torch.complex128 else gj.astype(np.complex64).astype(np.complex128)
+    want = oracle.apply_within_adjoint(g["site"], g["kind"], g["coef"], rows, rows, g_used, 1)
+    scale = _adjoint_scale(g["site"], g["kind"], g["coef"], 1, rows, rows, g_used)
+    tol = 1e-12 if dtype == torch.complex128 else 1e-6
+    assert np.all(np.abs(gi.to(torch.complex128).cpu().numpy() - want) <= tol * scale + 1e-300)
