@@ -122,6 +122,7 @@ __device__ __forceinline__ void comp_cmul_add(CompSum& re, CompSum& im, float4 c
 // Values of the looked-up rows sit in val[u] for unique key u of lookup.
 template <int W, bool CONJ>
 struct GatherF64 : VisitorBase {
+    static constexpr bool kTiledDense = true;
     HashView lookup;         // hash set over the unique keys of the looked-up row set
     const double2* val;      // one amplitude per unique looked-up key
     const double2* coef;     // coefficients of the walked part
@@ -209,6 +210,7 @@ struct GatherF64 : VisitorBase {
 
 template <int W, bool CONJ>
 struct GatherF32C : VisitorBase {
+    static constexpr bool kTiledDense = true;
     HashView lookup;
     const float2* val;
     const float4* coef32;
@@ -313,6 +315,7 @@ struct DiagonalF64 : VisitorBase {
 // FP32C forms the products in FP32 (exact two-products), FP64 otherwise.
 template <int W, bool CONJ, bool F32>
 struct Scatter : VisitorBase {
+    static constexpr bool kTiledDense = true;
     HashView lookup;        // output-side row set
     const void* val;        // amplitude per first row of the walked side (double2, or float2 for F32)
     const int32_t* unique;  // walk index -> first row of the walked key
@@ -648,7 +651,11 @@ int launch_walk(const V& v, const HashRows& walk, const PartView& part, const Pa
     if (choose_walk(part, walk.n, false) == Walk::kGrouped) {
         QMBX_KERNEL(group, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
     } else {
-        QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+        if constexpr (V::kTiledDense && W <= 2) {
+            QMBX_KERNEL(group, s, enumerate_dense_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+        } else {
+            QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(v, src, walk.count, walk.n, part, diag));
+        }
     }
     QMBX_LAUNCH_CHECK("apply_within enumeration");
     return QMBX_OK;
@@ -1170,6 +1177,37 @@ __global__ void log_poison_kernel(const LogGate* __restrict__ g, int64_t n, doub
 // converts to FP64 once per run: GB300 issues FP64 arithmetic at a small
 // fraction of the FP32 rate, and per-record FP64 adds and shuffles made the
 // FP64 pipe this kernel's bound.
+// The IEEE 754 double equal to x, formed with integer operations: a
+// conversion instruction would run on the FP64 pipe, which GB300 issues at a
+// small fraction of the FP32 rate and holds for tens of cycles a warp
+// instruction whatever its active mask.
+__device__ __forceinline__ double widen(float x) {
+    const uint32_t u = __float_as_uint(x);
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    const uint32_t ex = (u >> 23) & 0xffu;
+    const uint64_t mant = u & 0x7fffffu;
+    uint64_t bits;
+    if (ex == 0xffu) {
+        bits = sign | (0x7ffull << 52) | (mant << 29);  // infinity, NaN (payload kept)
+    } else if (ex != 0) {
+        bits = sign | ((uint64_t)(ex + 896u) << 52) | (mant << 29);  // normal: exponent bias 127 -> 1023
+    } else if (mant == 0) {
+        bits = sign;  // signed zero
+    } else {
+        // subnormal mant * 2^-149 with leading bit p: 2^(p - 149) (1 + f), normal as a double
+        const int p = 31 - __clz((unsigned)mant);
+        bits = sign | ((uint64_t)(p + 874) << 52) | ((mant << (52 - p)) & ((1ull << 52) - 1));
+    }
+    return __longlong_as_double((long long)bits);
+}
+
+// Add a compensated FP32 sum to an FP64 value in memory: head and tail go as
+// two FP64 atomics (executed in L2), so no FP64 arithmetic runs on the SM.
+__device__ __forceinline__ void atomic_add_comp(double* p, const CompSum& a) {
+    if (a.s != 0.f) atomicAdd(p, widen(a.s));
+    if (a.c != 0.f) atomicAdd(p, widen(a.c));
+}
+
 __device__ __forceinline__ void run_add_f32(CompSum& a, float s2, float c2) {
     float e;
     two_sum(a.s, s2, a.s, e);
@@ -1222,8 +1260,8 @@ __global__ void log_adjoint_kernel(const int4* __restrict__ hits, const LogHead*
         if (dir != 0) {
             // the walked rows were the inputs: neighbouring records add into different rows
             if (live) {
-                atomicAdd(&res[out].x, re.value());
-                atomicAdd(&res[out].y, im.value());
+                atomic_add_comp(&res[out].x, re);
+                atomic_add_comp(&res[out].y, im);
             }
             return;
         }
@@ -1238,8 +1276,8 @@ __global__ void log_adjoint_kernel(const int4* __restrict__ hits, const LogHead*
             }
         }
         if (last) {
-            atomicAdd(&res[out].x, re.value());
-            atomicAdd(&res[out].y, im.value());
+            atomic_add_comp(&res[out].x, re);
+            atomic_add_comp(&res[out].y, im);
         }
     } else {
         double re = 0.0, im = 0.0;

@@ -186,15 +186,15 @@ __device__ __forceinline__ int64_t hash_find(const HashView& h, const Key<W>& ke
     for (uint64_t probe = 0; probe <= h.mask; probe += kBucket) {
         const uint32_t* bucket = h.slots + 2 * b;
         const uint4 t4 = __ldg(reinterpret_cast<const uint4*>(bucket));
-        const uint32_t tag[kBucket] = {t4.x, t4.y, t4.z, t4.w};
-        bool open = false;
-#pragma unroll
-        for (int k = 0; k < kBucket; ++k) {
-            open |= tag[k] == kEmptyTag;
-            if (tag[k] == fp) {
-                const uint32_t row = __ldg(bucket + kBucket + k);
-                if (row != kEmptyRow && key_eq<W>(load_key<W>(h.keys, (int64_t)row), key)) return (int64_t)row;
-            }
+        // the four fingerprints compared at once: a miss (no match, an empty slot) costs one branch
+        const bool open = (t4.x == kEmptyTag) | (t4.y == kEmptyTag) | (t4.z == kEmptyTag) | (t4.w == kEmptyTag);
+        unsigned match = (unsigned)(t4.x == fp) | ((unsigned)(t4.y == fp) << 1) | ((unsigned)(t4.z == fp) << 2) |
+                         ((unsigned)(t4.w == fp) << 3);
+        while (match != 0) {
+            const int k = __ffs(match) - 1;
+            match &= match - 1;
+            const uint32_t row = __ldg(bucket + kBucket + k);
+            if (row != kEmptyRow && key_eq<W>(load_key<W>(h.keys, (int64_t)row), key)) return (int64_t)row;
         }
         if (open) return -1;
         b = (b + kBucket) & h.mask;
@@ -221,6 +221,7 @@ struct PartView {
     int64_t n_nonempty;
     int64_t n;
     int wide;                  // groups are large: walk each with lanes over its terms
+    const uint4* narrow;       // (mask, val, flip, par) >> 32 of every term (tables of <= 32 sites), or NULL
 };
 
 inline PartView part_view(const void* table_host, const void* table_dev, int which) {
@@ -242,6 +243,7 @@ inline PartView part_view(const void* table_host, const void* table_dev, int whi
     v.n_nonempty = p.n_nonempty;
     v.n = p.n;
     v.wide = p.wide_groups;
+    v.narrow = p.off_narrow != 0 ? reinterpret_cast<const uint4*>(base + p.off_narrow) : nullptr;
     return v;
 }
 
@@ -402,6 +404,7 @@ struct VisitorBase {
     template <class Acc, class K>
     __device__ __forceinline__ void flush(Acc&, int64_t, const K&) const {}
     static constexpr int kShared = 0;
+    static constexpr bool kTiledDense = false;  // tiled walks may run as enumerate_dense_kernel (W <= 2)
     static constexpr bool kBatched = false;  // hits are queued and processed by apply_hit with full lanes
     static constexpr bool kStateless = false; // pivot walks: hits carry their row and need no per-row state
     template <class Acc>
@@ -429,8 +432,8 @@ struct VisitorBase {
 // (cheap, branch-free, all lanes reading the same term) and then visits only
 // the terms that applied.
 template <int W, class V, class Src>
-__global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const int* __restrict__ n_rows,
-                                                             int64_t n_max, PartView off, PartView diag) {
+__device__ __forceinline__ void enumerate_rows(const V& v, const Src& src, const int* __restrict__ n_rows,
+                                               int64_t n_max, const PartView& off, const PartView& diag) {
     __shared__ TermTile<W> tile;
     const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
     if ((int64_t)blockIdx.x * blockDim.x >= n) return;
@@ -478,6 +481,23 @@ __global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const
     if (live) v.finish(acc, row, c);
     __syncthreads();
     v.block_flush(sh);
+}
+
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads) enumerate_kernel(V v, Src src, const int* __restrict__ n_rows,
+                                                             int64_t n_max, PartView off, PartView diag) {
+    enumerate_rows<W>(v, src, n_rows, n_max, off, diag);
+}
+
+// The same walk with five resident blocks per SM asked of the compiler (at
+// most 48 registers a thread), for visitors with kTiledDense and keys of one
+// or two words, which fit that without spills: their row lookups get 40
+// warps per SM to hide L2 latency behind instead of 32 (C4 forward walk
+// 1.23 -> 1.15 ms on GB300).
+template <int W, class V, class Src>
+__global__ void __launch_bounds__(kThreads, 5) enumerate_dense_kernel(V v, Src src, const int* __restrict__ n_rows,
+                                                                      int64_t n_max, PartView off, PartView diag) {
+    enumerate_rows<W>(v, src, n_rows, n_max, off, diag);
 }
 
 // ---------------------------------------------------------------------------
@@ -538,16 +558,32 @@ __device__ __forceinline__ void load_apply(TermRec<W>& r, const PartView& pv, in
     }
 }
 
+// The whole record of term t from its narrow form (one 16-byte load; the
+// part must have one: W == 1 and pv.narrow set).
+template <int W>
+__device__ __forceinline__ void load_narrow(TermRec<W>& r, const PartView& pv, int64_t t) {
+    const uint4 q = __ldg(pv.narrow + t);
+    r.m[0] = (uint64_t)q.x << 32;
+    r.m[1] = (uint64_t)q.y << 32;
+    r.m[2] = (uint64_t)q.z << 32;
+    r.m[3] = (uint64_t)q.w << 32;
+}
+
 // Hits of batched visitors wait in a per-warp shared queue until 32 have
 // gathered, then every lane processes one: the floating-point work of a hit
 // (FP64 on GB300 issues at a small fraction of the FP32 rate) then runs with
 // all lanes active instead of once per divergent warp iteration.
+// Candidates of a batched walk wait in a per-warp ring of kCandRing entries:
+// fewer than 32 wait between steps, and a step adds at most 64.
+constexpr int kCandRing = 128;
+
 struct HitQueue {
     int2* q;         // 64 entries: (slot | parity << 31, looked-up row)
     int count;       // warp-uniform
-    uint64_t* ckey;  // 64 candidate images (W words each) waiting for their lookup
+    uint64_t* ckey;  // ring of kCandRing candidate images (W words each) waiting for their lookup
     int* cmeta;      // slot | parity << 31 of each candidate
-    int ccount;      // warp-uniform
+    int ccount;      // warp-uniform: candidates waiting
+    int chead;       // warp-uniform: ring position of the oldest waiting candidate
 };
 
 template <class V>
@@ -583,9 +619,16 @@ template <int W, bool DIAG, class V>
 __device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, const Key<W>& c, const PartView& pv,
                                           int64_t t, int2& h) {
     TermRec<W> r;
-    load_test<W>(r, pv, t);
-    if (!r.applies(c)) return false;
-    load_apply<W>(r, pv, t);
+    bool narrow = false;
+    if constexpr (W == 1) narrow = pv.narrow != nullptr;
+    if (narrow) {
+        load_narrow<W>(r, pv, t);
+        if (!r.applies(c)) return false;
+    } else {
+        load_test<W>(r, pv, t);
+        if (!r.applies(c)) return false;
+        load_apply<W>(r, pv, t);
+    }
     Key<W> img;
     const int par = r.image(c, img);
     if (DIAG) {
@@ -599,32 +642,66 @@ __device__ __forceinline__ bool test_term(const V& v, typename V::Acc& acc, cons
     }
 }
 
-// Look up the first n (<= 32) queued candidates, one per lane, queue the
-// hits, and move the remaining candidates to the front.
+// Look up the n (<= 32) oldest queued candidates, one per lane, and queue
+// the hits.  The candidates sit in a ring: the flush only advances its head,
+// and the __syncwarp orders its reads before the appends that reuse the
+// entries.
 template <int W, class V>
 __device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& acc, HitQueue& hq, int lane, int n) {
     int2 h = make_int2(0, 0);
     bool hit = false;
     if (lane < n) {
+        const int at = (hq.chead + lane) & (kCandRing - 1);
         Key<W> img;  // plain loads: the candidate queue is in shared memory
 #pragma unroll
-        for (int q = 0; q < W; ++q) img.w[q] = hq.ckey[lane * W + q];
+        for (int q = 0; q < W; ++q) img.w[q] = hq.ckey[at * W + q];
         const int64_t pos = hash_find<W>(v.lookup, img);
         if (pos >= 0) {
             hit = true;
-            h = make_int2(hq.cmeta[lane], (int)pos);
+            h = make_int2(hq.cmeta[at], (int)pos);
         }
     }
     __syncwarp();
-    const int rest = hq.ccount - n;
-    if (lane < rest) {
-#pragma unroll
-        for (int q = 0; q < W; ++q) hq.ckey[lane * W + q] = hq.ckey[(n + lane) * W + q];
-        hq.cmeta[lane] = hq.cmeta[n + lane];
-    }
-    __syncwarp();
-    hq.ccount = rest;
+    hq.chead = (hq.chead + n) & (kCandRing - 1);
+    hq.ccount -= n;
     queue_push(v, acc, hq, lane, hit, h);
+}
+
+// walk_group_lanes of a batched visitor over narrow records (one-word keys,
+// every mask in the high half): one 16-byte load a term and 32-bit tests
+// against the row's high half; the images are formed in the full word.
+template <class V>
+__device__ __forceinline__ void walk_group_narrow(const V& v, typename V::Acc& acc, const Key<1>& c,
+                                                  const PartView& pv, int2 se, int lane, HitQueue& hq) {
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t hi = (uint32_t)(c.w[0] >> 32);
+    for (int base = se.x; base < se.y; base += 64) {
+        const int t0 = base + lane, t1 = base + 32 + lane;
+        const bool in0 = t0 < se.y, in1 = t1 < se.y;
+        uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = make_uint4(0u, 0u, 0u, 0u);
+        if (in0) q0 = __ldg(pv.narrow + t0);
+        if (in1) q1 = __ldg(pv.narrow + t1);
+        const bool app0 = in0 && ((hi ^ q0.y) & q0.x) == 0u;
+        const bool app1 = in1 && ((hi ^ q1.y) & q1.x) == 0u;
+        const unsigned m0 = __ballot_sync(0xffffffffu, app0);
+        const unsigned m1 = __ballot_sync(0xffffffffu, app1);
+        if ((m0 | m1) == 0) continue;
+        // both terms of every lane appended in one step: the first terms, then the second
+        const int tail = hq.chead + hq.ccount, n0 = __popc(m0);
+        if (app0) {
+            const int at = (tail + __popc(m0 & lt)) & (kCandRing - 1);
+            hq.ckey[at] = c.w[0] ^ ((uint64_t)q0.z << 32);
+            hq.cmeta[at] = t0 | ((__popc(hi & q0.w) & 1) << 31);
+        }
+        if (app1) {
+            const int at = (tail + n0 + __popc(m1 & lt)) & (kCandRing - 1);
+            hq.ckey[at] = c.w[0] ^ ((uint64_t)q1.z << 32);
+            hq.cmeta[at] = t1 | ((__popc(hi & q1.w) & 1) << 31);
+        }
+        hq.ccount += n0 + __popc(m1);
+        __syncwarp();
+        while (hq.ccount >= 32) candidates_flush<1>(v, acc, hq, lane, 32);
+    }
 }
 
 // Walk one group: lanes over its terms (warp-uniform bounds, so work can be
@@ -634,6 +711,12 @@ template <int W, bool DIAG, class V>
 __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& acc, const Key<W>& c,
                                                  const PartView& pv, int64_t g, int lane, HitQueue& hq) {
     const int2 se = __ldg(pv.groups + g);
+    if constexpr (V::kBatched && !DIAG && W == 1) {
+        if (pv.narrow != nullptr) {
+            walk_group_narrow(v, acc, c, pv, se, lane, hq);
+            return;
+        }
+    }
     if constexpr (V::kBatched && !DIAG) {
         const unsigned lt = (1u << lane) - 1u;
         // two terms per lane per step: both records are loaded before either is tested
@@ -649,25 +732,27 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
             if (in1) load_apply<W>(r1, pv, t1);
             const bool app0 = in0 && r0.applies(c);
             const bool app1 = in1 && r1.applies(c);
+            const unsigned m0 = __ballot_sync(0xffffffffu, app0);
+            const unsigned m1 = __ballot_sync(0xffffffffu, app1);
+            if ((m0 | m1) == 0) continue;
+            // both terms of every lane appended in one step: the first terms, then the second
+            const int tail = hq.chead + hq.ccount, n0 = __popc(m0);
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
-                const TermRec<W>& rec = half ? r1 : r0;
-                const int t = half ? t1 : t0;
                 const bool app = half ? app1 : app0;
-                const unsigned m = __ballot_sync(0xffffffffu, app);
-                if (m == 0) continue;
                 if (app) {
+                    const TermRec<W>& rec = half ? r1 : r0;
                     Key<W> img;
                     const int par = rec.image(c, img);
-                    const int at = hq.ccount + __popc(m & lt);
+                    const int at = (tail + (half ? n0 + __popc(m1 & lt) : __popc(m0 & lt))) & (kCandRing - 1);
 #pragma unroll
                     for (int q = 0; q < W; ++q) hq.ckey[at * W + q] = img.w[q];
-                    hq.cmeta[at] = t | (par << 31);
+                    hq.cmeta[at] = (half ? t1 : t0) | (par << 31);
                 }
-                hq.ccount += __popc(m);
-                __syncwarp();
-                if (hq.ccount >= 32) candidates_flush<W>(v, acc, hq, lane, 32);
             }
+            hq.ccount += n0 + __popc(m1);
+            __syncwarp();
+            while (hq.ccount >= 32) candidates_flush<W>(v, acc, hq, lane, 32);
         }
     } else {
         for (int64_t base = se.x; base < se.y; base += 32) {
@@ -806,8 +891,8 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
                                                            int64_t n_max, PartView off, PartView diag) {
     __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
     __shared__ int2 hitq[kWarpsPerBlock][64];
-    __shared__ uint64_t candkey[V::kBatched ? kWarpsPerBlock : 1][64 * W];
-    __shared__ int candmeta[V::kBatched ? kWarpsPerBlock : 1][64];
+    __shared__ uint64_t candkey[V::kBatched ? kWarpsPerBlock : 1][kCandRing * W];
+    __shared__ int candmeta[V::kBatched ? kWarpsPerBlock : 1][kCandRing];
     v.block_init(sh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -818,7 +903,7 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
         const Key<W> c = src.get(row);
         typename V::Acc acc;
         v.init(acc, row, c, sh);
-        HitQueue hq{hitq[warp], 0, candkey[V::kBatched ? warp : 0], candmeta[V::kBatched ? warp : 0], 0};
+        HitQueue hq{hitq[warp], 0, candkey[V::kBatched ? warp : 0], candmeta[V::kBatched ? warp : 0], 0, 0};
         walk_part<W, false>(v, acc, c, off, lane, hq);
         if constexpr (V::kBatched) {
             if (hq.ccount > 0) candidates_flush<W>(v, acc, hq, lane, hq.ccount);
@@ -855,7 +940,7 @@ __global__ void __launch_bounds__(kThreads) grouped_split_kernel(V v, Src src, i
         const Key<W> c = src.get(row);
         typename V::Acc acc;
         v.init(acc, row, c, sh);
-        HitQueue hq{hitq[warp], 0, nullptr, nullptr, 0};
+        HitQueue hq{hitq[warp], 0, nullptr, nullptr, 0, 0};
         walk_part<W, false>(v, acc, c, off, lane, hq, part, split);
         walk_part<W, true>(v, acc, c, diag, lane, hq, part, split);
         v.reduce(acc);

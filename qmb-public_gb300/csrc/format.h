@@ -39,13 +39,16 @@
 // (mask, val) and the apply pair (flip, par): lanes that read consecutive
 // terms of one word read consecutive 16-byte pairs (fully coalesced loads),
 // and a walk that tests terms one at a time reads the apply pair only for
-// terms whose test passed.
+// terms whose test passed.  Tables of at most 32 sites (n_qubytes <= 4) also
+// hold every term's four masks narrowed to their high 32 bits in one 16-byte
+// record, which the grouped walks read instead: half the bytes a term, one
+// load, and 32-bit tests.
 #pragma once
 
 #include <stdint.h>
 
 #define QMBX_MAGIC 0x58424D51u  // "QMBX"
-#define QMBX_TABLE_VERSION 6u
+#define QMBX_TABLE_VERSION 7u
 #define QMBX_MAX_WORDS 4
 #define QMBX_ALIGN 256
 
@@ -64,6 +67,8 @@ struct qmbx_table_part {
     uint64_t off_pair_ne;    // uint64[64W][W]  for position p: positions q > p with a non-empty pair group
     uint64_t off_nonempty;   // int32[n_groups][4]: (start, end, p, q) of each non-empty group in id order
                              // (p, q the pivot key positions, -1 when absent; first n_nonempty rows valid)
+    uint64_t off_narrow;     // uint32[n][4]: (mask, val, flip, par) >> 32 of every term, present (non-zero)
+                             // when n_sites <= 32: one key word whose low half is always zero
     int64_t n_groups;        // 1 + 64W + 64W(64W-1)/2
     int64_t n_nonempty;      // groups holding at least one term
     int32_t wide_groups;     // 1 when non-empty groups hold 8 or more terms on average

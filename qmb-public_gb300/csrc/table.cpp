@@ -141,7 +141,7 @@ struct Layout {
     qmbx_table_header h;
 };
 
-void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
+void layout_part(qmbx_table_part& p, int64_t n, int words, bool narrow, uint64_t& cursor) {
     p.n = n;
     p.n_groups = qmbx_group_count(words);
     uint64_t un = (uint64_t)n;
@@ -165,6 +165,11 @@ void layout_part(qmbx_table_part& p, int64_t n, int words, uint64_t& cursor) {
     cursor = align_up(cursor + (uint64_t)64 * words * words * 8);
     p.off_nonempty = cursor;
     cursor = align_up(cursor + (uint64_t)p.n_groups * 16);
+    p.off_narrow = 0;
+    if (narrow) {
+        p.off_narrow = cursor;
+        cursor = align_up(cursor + un * 16);
+    }
 }
 
 // Pivot group of a compiled term (see format.h).
@@ -246,9 +251,10 @@ qmbx_table_header make_header(int64_t n_terms, int32_t n_qubytes, int32_t partic
     h.n_terms = n_terms;
     h.n_live = n_off + n_diag;
     uint64_t cursor = align_up(sizeof(qmbx_table_header));
-    layout_part(h.part[QMBX_PART_FWD], n_off, h.n_words, cursor);
-    layout_part(h.part[QMBX_PART_ADJ], n_off, h.n_words, cursor);
-    layout_part(h.part[QMBX_PART_DIAG], n_diag, h.n_words, cursor);
+    const bool narrow = h.n_sites <= 32;  // every mask in the high half of key word 0
+    layout_part(h.part[QMBX_PART_FWD], n_off, h.n_words, narrow, cursor);
+    layout_part(h.part[QMBX_PART_ADJ], n_off, h.n_words, narrow, cursor);
+    layout_part(h.part[QMBX_PART_DIAG], n_diag, h.n_words, narrow, cursor);
     h.total_bytes = cursor;
     return h;
 }
@@ -295,6 +301,13 @@ void write_term(char* blob, const qmbx_table_part& p, int words, int64_t slot, c
     c32[3] = (float)(im - (double)im_hi);
     reinterpret_cast<int32_t*>(blob + p.off_orig)[slot] = (int32_t)orig;
     reinterpret_cast<float*>(blob + p.off_norm)[slot] = (float)(re * re + im * im);
+    if (p.off_narrow != 0) {
+        uint32_t* nr = reinterpret_cast<uint32_t*>(blob + p.off_narrow) + slot * 4;
+        nr[0] = (uint32_t)(c.mask[0] >> 32);
+        nr[1] = (uint32_t)(c.val[0] >> 32);
+        nr[2] = (uint32_t)(c.flip[0] >> 32);
+        nr[3] = (uint32_t)(c.par[0] >> 32);
+    }
 }
 
 }  // namespace
@@ -302,7 +315,7 @@ void write_term(char* blob, const qmbx_table_part& p, int words, int64_t slot, c
 
 using namespace qmbx;
 
-extern "C" int qmbx_version(void) { return 10000; }
+extern "C" int qmbx_version(void) { return 10001; }
 
 extern "C" const char* qmbx_last_error(void) { return g_last_error.c_str(); }
 

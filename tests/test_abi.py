@@ -45,7 +45,8 @@ def test_version_and_no_error(lib):
 class Part(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("off_test", ctypes.c_uint64), ("off_apply", ctypes.c_uint64), ("off_coef", ctypes.c_uint64), ("off_coef32", ctypes.c_uint64), ("off_orig", ctypes.c_uint64),
                 ("off_norm", ctypes.c_uint64), ("off_groups", ctypes.c_uint64), ("off_single_ne", ctypes.c_uint64),
-                ("off_pair_ne", ctypes.c_uint64), ("off_nonempty", ctypes.c_uint64), ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
+                ("off_pair_ne", ctypes.c_uint64), ("off_nonempty", ctypes.c_uint64), ("off_narrow", ctypes.c_uint64),
+                ("n_groups", ctypes.c_int64), ("n_nonempty", ctypes.c_int64),
                 ("wide_groups", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
@@ -134,6 +135,20 @@ def check_groups(blob, h, which, part):
                 assert g == 0
 
 
+def check_narrow(blob, h, which, part):
+    """Tables of at most 32 sites hold (mask, val, flip, par) >> 32 of every term; the low halves are zero."""
+    p = h.part[which]
+    test, apply, _, _ = part
+    if h.n_sites > 32:
+        assert p.off_narrow == 0
+        return
+    assert p.off_narrow != 0 and p.off_narrow % 16 == 0
+    narrow = np.frombuffer(blob, dtype=np.uint32, count=4 * p.n, offset=p.off_narrow).reshape(p.n, 4)
+    full = np.stack([test[:, 0, 0], test[:, 0, 1], apply[:, 0, 0], apply[:, 0, 1]], axis=1)
+    assert np.all(full & np.uint64(0xFFFFFFFF) == 0)
+    assert np.array_equal((full >> np.uint64(32)).astype(np.uint32), narrow)
+
+
 def closed_form(test, apply, key):
     for q, word in enumerate(key):
         mask, val = int(test[q, 0]), int(test[q, 1])
@@ -166,6 +181,11 @@ def test_compiled_terms_reproduce_the_operator_walk(lib, case):
     assert sorted(fwd[3].tolist()) == sorted(adj[3].tolist())
     for which, part in ((0, fwd), (1, adj), (2, diag)):
         check_groups(blob, h, which, part)
+        check_narrow(blob, h, which, part)
+    # the same terms on rows of more than 32 sites carry no narrow records
+    wide = compile_table(lib, site, kind, coef, 5, pc)
+    hw = Header.from_buffer_copy(wide[:ctypes.sizeof(Header)].tobytes())
+    assert all(hw.part[k].off_narrow == 0 for k in range(3))
     for t in range(site.shape[0]):
         ok_any = any(oracle.apply_term(site[t], kind[t], r, pc)[0] for r in rows[:40])
         if ok_any:
