@@ -573,14 +573,16 @@ __device__ __forceinline__ void load_narrow(TermRec<W>& r, const PartView& pv, i
 // gathered, then every lane processes one: the floating-point work of a hit
 // (FP64 on GB300 issues at a small fraction of the FP32 rate) then runs with
 // all lanes active instead of once per divergent warp iteration.
-// Candidates of a batched walk wait in a per-warp ring of kCandRing entries:
-// fewer than 32 wait between steps, and a step adds at most 64.
-constexpr int kCandRing = 128;
+// Candidates of a batched walk wait in a per-warp ring: fewer than 32 wait
+// between steps, and a step adds at most 32 per term a lane takes (two, or
+// kNarrowTerms in the narrow walk of one-word keys).
+constexpr int kNarrowTerms = 4;
+__host__ __device__ constexpr int cand_ring(int W) { return W == 1 ? (kNarrowTerms > 2 ? 256 : 128) : 128; }
 
 struct HitQueue {
     int2* q;         // 64 entries: (slot | parity << 31, looked-up row)
     int count;       // warp-uniform
-    uint64_t* ckey;  // ring of kCandRing candidate images (W words each) waiting for their lookup
+    uint64_t* ckey;  // ring of cand_ring(W) candidate images (W words each) waiting for their lookup
     int* cmeta;      // slot | parity << 31 of each candidate
     int ccount;      // warp-uniform: candidates waiting
     int chead;       // warp-uniform: ring position of the oldest waiting candidate
@@ -651,7 +653,7 @@ __device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& ac
     int2 h = make_int2(0, 0);
     bool hit = false;
     if (lane < n) {
-        const int at = (hq.chead + lane) & (kCandRing - 1);
+        const int at = (hq.chead + lane) & (cand_ring(W) - 1);
         Key<W> img;  // plain loads: the candidate queue is in shared memory
 #pragma unroll
         for (int q = 0; q < W; ++q) img.w[q] = hq.ckey[at * W + q];
@@ -662,7 +664,7 @@ __device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& ac
         }
     }
     __syncwarp();
-    hq.chead = (hq.chead + n) & (kCandRing - 1);
+    hq.chead = (hq.chead + n) & (cand_ring(W) - 1);
     hq.ccount -= n;
     queue_push(v, acc, hq, lane, hit, h);
 }
@@ -673,32 +675,41 @@ __device__ __forceinline__ void candidates_flush(const V& v, typename V::Acc& ac
 template <class V>
 __device__ __forceinline__ void walk_group_narrow(const V& v, typename V::Acc& acc, const Key<1>& c,
                                                   const PartView& pv, int2 se, int lane, HitQueue& hq) {
+    constexpr int K = kNarrowTerms;
+    constexpr int kRing = cand_ring(1);
     const unsigned lt = (1u << lane) - 1u;
     const uint32_t hi = (uint32_t)(c.w[0] >> 32);
-    for (int base = se.x; base < se.y; base += 64) {
-        const int t0 = base + lane, t1 = base + 32 + lane;
-        const bool in0 = t0 < se.y, in1 = t1 < se.y;
-        uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = make_uint4(0u, 0u, 0u, 0u);
-        if (in0) q0 = __ldg(pv.narrow + t0);
-        if (in1) q1 = __ldg(pv.narrow + t1);
-        const bool app0 = in0 && ((hi ^ q0.y) & q0.x) == 0u;
-        const bool app1 = in1 && ((hi ^ q1.y) & q1.x) == 0u;
-        const unsigned m0 = __ballot_sync(0xffffffffu, app0);
-        const unsigned m1 = __ballot_sync(0xffffffffu, app1);
-        if ((m0 | m1) == 0) continue;
-        // both terms of every lane appended in one step: the first terms, then the second
-        const int tail = hq.chead + hq.ccount, n0 = __popc(m0);
-        if (app0) {
-            const int at = (tail + __popc(m0 & lt)) & (kCandRing - 1);
-            hq.ckey[at] = c.w[0] ^ ((uint64_t)q0.z << 32);
-            hq.cmeta[at] = t0 | ((__popc(hi & q0.w) & 1) << 31);
+    for (int base = se.x; base < se.y; base += 32 * K) {
+        // K terms a lane, all records loaded before any is tested
+        uint4 q[K];
+        bool app[K];
+        unsigned m[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int t = base + 32 * k + lane;
+            q[k] = make_uint4(0u, 0u, 0u, 0u);
+            if (t < se.y) q[k] = __ldg(pv.narrow + t);
         }
-        if (app1) {
-            const int at = (tail + n0 + __popc(m1 & lt)) & (kCandRing - 1);
-            hq.ckey[at] = c.w[0] ^ ((uint64_t)q1.z << 32);
-            hq.cmeta[at] = t1 | ((__popc(hi & q1.w) & 1) << 31);
+        unsigned any = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            app[k] = base + 32 * k + lane < se.y && ((hi ^ q[k].y) & q[k].x) == 0u;
+            m[k] = __ballot_sync(0xffffffffu, app[k]);
+            any |= m[k];
         }
-        hq.ccount += n0 + __popc(m1);
+        if (any == 0) continue;
+        // every lane's terms appended in one step, term k of all lanes after term k - 1
+        int at0 = hq.chead + hq.ccount;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (app[k]) {
+                const int at = (at0 + __popc(m[k] & lt)) & (kRing - 1);
+                hq.ckey[at] = c.w[0] ^ ((uint64_t)q[k].z << 32);
+                hq.cmeta[at] = (base + 32 * k + lane) | ((__popc(hi & q[k].w) & 1) << 31);
+            }
+            at0 += __popc(m[k]);
+        }
+        hq.ccount = at0 - hq.chead;
         __syncwarp();
         while (hq.ccount >= 32) candidates_flush<1>(v, acc, hq, lane, 32);
     }
@@ -744,7 +755,7 @@ __device__ __forceinline__ void walk_group_lanes(const V& v, typename V::Acc& ac
                     const TermRec<W>& rec = half ? r1 : r0;
                     Key<W> img;
                     const int par = rec.image(c, img);
-                    const int at = (tail + (half ? n0 + __popc(m1 & lt) : __popc(m0 & lt))) & (kCandRing - 1);
+                    const int at = (tail + (half ? n0 + __popc(m1 & lt) : __popc(m0 & lt))) & (cand_ring(W) - 1);
 #pragma unroll
                     for (int q = 0; q < W; ++q) hq.ckey[at * W + q] = img.w[q];
                     hq.cmeta[at] = (half ? t1 : t0) | (par << 31);
@@ -891,8 +902,8 @@ __global__ void __launch_bounds__(kThreads) grouped_kernel(V v, Src src, const i
                                                            int64_t n_max, PartView off, PartView diag) {
     __shared__ int sh[V::kShared > 0 ? V::kShared : 1];
     __shared__ int2 hitq[kWarpsPerBlock][64];
-    __shared__ uint64_t candkey[V::kBatched ? kWarpsPerBlock : 1][kCandRing * W];
-    __shared__ int candmeta[V::kBatched ? kWarpsPerBlock : 1][kCandRing];
+    __shared__ uint64_t candkey[V::kBatched ? kWarpsPerBlock : 1][cand_ring(W) * W];
+    __shared__ int candmeta[V::kBatched ? kWarpsPerBlock : 1][cand_ring(W)];
     v.block_init(sh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
