@@ -64,9 +64,12 @@ struct CompSum {
     }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
     // Combine the lanes' pairs: two-sum of the leading parts, plain sum of the tails.
-    __device__ __forceinline__ void warp_reduce() {
+    __device__ __forceinline__ void warp_reduce() { group_reduce<32>(); }
+    // The same within aligned groups of L lanes (every lane of a group ends with its total).
+    template <int L>
+    __device__ __forceinline__ void group_reduce() {
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
+        for (int d = L / 2; d > 0; d >>= 1) {
             float s2 = __shfl_xor_sync(0xffffffffu, s, d);
             float c2 = __shfl_xor_sync(0xffffffffu, c, d);
             float e;
@@ -539,6 +542,19 @@ struct DiagAdd : VisitorBase {
             a.dim = warp_sum(a.dim);
         }
     }
+    template <int L>
+    __device__ __forceinline__ void reduce_lanes(Acc& a) const {
+        if (F32) {
+            a.fre.template group_reduce<L>();
+            a.fim.template group_reduce<L>();
+        } else {
+#pragma unroll
+            for (int d = L / 2; d > 0; d >>= 1) {
+                a.dre += __shfl_xor_sync(0xffffffffu, a.dre, d);
+                a.dim += __shfl_xor_sync(0xffffffffu, a.dim, d);
+            }
+        }
+    }
     __device__ __forceinline__ void finish(Acc& a, int64_t u, const Key<W>& c) const {
         if (F32) {
             a.dre = a.fre.value();
@@ -673,7 +689,11 @@ int launch_diag(const D& dv, const HashRows& walk, const PartView& part, const P
     if (choose_walk(diag, walk.n, false) == Walk::kGrouped) {
         QMBX_KERNEL(group, s, grouped_kernel<W><<<grouped_grid(walk.n), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
     } else {
-        QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+        if (diag_lanes(walk.n) == 8) {
+            QMBX_KERNEL(group, s, diag_split_kernel<W, 8><<<grid_for(walk.n * 8, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, diag));
+        } else {
+            QMBX_KERNEL(group, s, enumerate_kernel<W><<<grid_for(walk.n, kThreads), kThreads, 0, s>>>(dv, src, walk.count, walk.n, none, diag));
+        }
     }
     QMBX_LAUNCH_CHECK("apply_within diagonal pass");
     return QMBX_OK;

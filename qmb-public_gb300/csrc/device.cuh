@@ -500,6 +500,55 @@ __global__ void __launch_bounds__(kThreads, 5) enumerate_dense_kernel(V v, Src s
     enumerate_rows<W>(v, src, n_rows, n_max, off, diag);
 }
 
+// The tiled walk of a diagonal part with each row shared by L lanes (lane
+// group g = threadIdx.x / L of the block): lane s of a group tests terms s,
+// s + L, ... of every staged tile, the group's sums are combined with
+// shuffles (the visitor's reduce_lanes<L>), and its first lane finishes the
+// row.  For diagonal passes over too few rows to fill the GPU with a thread
+// each (C2's 20,000 rows are 79 blocks of 256).  The visitor's init must read
+// nothing: it also runs for the lanes past the last row.
+template <int W, int L, class V, class Src>
+__global__ void __launch_bounds__(kThreads) diag_split_kernel(V v, Src src, const int* __restrict__ n_rows,
+                                                              int64_t n_max, PartView diag) {
+    static_assert(L == 8, "a row is shared by 8 lanes");
+    __shared__ TermTile<W> tile;
+    const int64_t n = n_rows ? (int64_t)*n_rows : n_max;
+    const int64_t first = (int64_t)blockIdx.x * (kThreads / L);
+    if (first >= n) return;  // the whole block is past the last row
+    const int sub = threadIdx.x % L;
+    const int64_t row = first + threadIdx.x / L;
+    const bool live = row < n;
+    Key<W> c;
+    if (live) {
+        c = src.get(row);
+    } else {
+#pragma unroll
+        for (int q = 0; q < W; ++q) c.w[q] = 0;
+    }
+    typename V::Acc acc;
+    v.init(acc, row, c, nullptr);
+    for (int64_t t0 = 0; t0 < diag.n; t0 += kTermTile) {
+        const int count = (int)(diag.n - t0 < kTermTile ? diag.n - t0 : kTermTile);
+        __syncthreads();
+        stage_tile<W>(tile, diag, t0, count);
+        __syncthreads();
+        if (!live) continue;
+        for (int k = sub; k < count; k += L) {
+            if (term_applies<W>(tile.m[k], c)) {
+                Key<W> img;
+                v.visit_diag(acc, c, term_image<W>(tile.m[k], c, img), t0 + k);
+            }
+        }
+    }
+    v.template reduce_lanes<L>(acc);
+    if (live && sub == 0) v.finish(acc, row, c);
+}
+
+// Lanes a row of a tiled diagonal pass is shared by: 8 below 40,000 rows
+// (C2's 20,000-row pass 40 -> 27 us on GB300), else 1 (the plain tiled
+// kernel; at 65,536 rows four lanes a row were slower, 125 -> 163 us).
+inline int diag_lanes(int64_t n_rows) { return n_rows < 40000 ? 8 : 1; }
+
 // ---------------------------------------------------------------------------
 // the grouped enumeration kernel: one warp per row, visiting only the pivot
 // groups whose sites the row occupies (see format.h).  Large groups are
