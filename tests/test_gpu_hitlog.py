@@ -148,3 +148,34 @@ def test_backward_on_the_same_rows(dtype, cuda_device):
     scale = _adjoint_scale(g["site"], g["kind"], g["coef"], 1, rows, rows, g_used)
     tol = 1e-12 if dtype == torch.complex128 else 1e-6
     assert np.all(np.abs(gi.to(torch.complex128).cpu().numpy() - want) <= tol * scale + 1e-300)
+
+
+@pytest.mark.parametrize("swap", [False, True])
+def test_replay_keeps_subnormal_sums(swap, cuda_device):
+    # The compensated FP32 replay widens its float run sums to FP64 with integer bit operations.
+    # A gradient scaled by 2^-140 makes every product and run sum an FP32 subnormal: they must
+    # reach the FP64 output, not be flushed or mis-scaled.  Each product of a subnormal keeps the
+    # subnormal grid (2^-149), so a row may differ from the FP64 oracle by its pair count times
+    # a few grid steps.
+    g = golden("ab_initio_6")
+    ci, cj = (g["configs_j"], g["configs_i"]) if swap else (g["configs_i"], g["configs_j"])
+    ham = _ham(g)
+    rng = np.random.default_rng(11)
+    psi = rng.standard_normal(ci.shape[0]) + 1j * rng.standard_normal(ci.shape[0])
+    gj = ((rng.standard_normal(cj.shape[0]) + 1j * rng.standard_normal(cj.shape[0])) * 2.0 ** -140).astype(np.complex64)
+    assert np.all(np.abs(gj.real) < 2.0 ** -126) and np.count_nonzero(gj.real) > cj.shape[0] // 2
+    dci, dcj = torch.from_numpy(ci).to(cuda_device), torch.from_numpy(cj).to(cuda_device)
+    p = torch.from_numpy(psi).to(cuda_device).to(torch.complex64)
+    _, record = ham._apply(dci, p, dcj, adjoint=False, log=True)
+    got = ham._adjoint_from_log(record, torch.from_numpy(gj).to(cuda_device), torch.complex128)
+    assert got is not None
+    got = got.cpu().numpy()
+    want = oracle.apply_within_adjoint(g["site"], g["kind"], g["coef"], ci, cj, gj.astype(np.complex128),
+                                       int(g["particle_cut"]))
+    ones = np.zeros_like(g["coef"])
+    ones[:, 0] = 1.0
+    pairs = np.abs(oracle.apply_within_adjoint(g["site"], g["kind"], ones, ci, cj, np.ones(cj.shape[0], np.complex128), 2))
+    assert np.all(np.abs(got - want) <= (pairs + 1.0) * 8 * 2.0 ** -149)
+    # nothing flushed to zero or scaled: the rows sum to the oracle's total magnitude
+    assert np.median(np.abs(want)) > 1e3 * 2.0 ** -149
+    assert np.sum(np.abs(got)) == pytest.approx(np.sum(np.abs(want)), rel=0.02)
